@@ -1,0 +1,264 @@
+"""Benchmark of the GB300 SCD engine: plain SCD on R-MAT scale 22 (edge factor
+16, a/b/c/d = .57/.19/.19/.05), one step = the whole pipeline of `convert` +
+`main-gpu` on one graph: device preprocessing (renumbering, sort/dedup,
+triangle counting, triangle filter, degree relabel, CSR), initial partition,
+initial WCC and refinement iterations until convergence, best labels ready.
+
+  value     E_in / step time with the edge list already resident in HBM
+            (CUDA events on the engine's stream)
+  e2e       the same through the C ABI with HOST buffers: pinned edge list
+            H2D inside the timed region, best labels D2H at the end
+  roofline  the dominant kernel (triangle counting) against measured HBM peak
+  cpu_baseline  the CPU oracle (restatement of the reference's CPU path) on a
+            bounded sample of the same workload (R-MAT scale 18, same a,b,c,d)
+
+`--impl reference` times the reference's CPU implementation instead (its own
+binaries when they were built from its sources, else the oracle restatement),
+each step a bounded sample of the same workload.  Single graph, so more GPUs
+run independent replicas (weak scaling, no collective).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _sub in ("het-scd_gb300", "oracle"):
+    sys.path.insert(0, os.path.join(ROOT, _sub))
+
+METRIC = "SCD edges/s end-to-end"
+UNIT = "edges/s"
+CPU_SAMPLE_SCALE = 18
+
+
+def algorithmic_tc_bytes(indices, adj):
+    """B_tc = 4*[(n+1) + m + sum over oriented edges u->v of (d+(u) + d+(v))] + 8n,
+    orientation from the larger to the smaller final id (degree-descending ids)."""
+    import numpy as np
+    n = len(indices) - 1
+    deg = np.diff(indices.astype(np.int64))
+    src = np.repeat(np.arange(n, dtype=np.int64), deg)
+    out = adj.astype(np.int64) < src
+    dplus = np.bincount(src[out], minlength=n)
+    m = int(out.sum())
+    s = int(dplus[src[out]].sum() + dplus[adj[out].astype(np.int64)].sum())
+    return 4 * ((n + 1) + m + s) + 8 * n, dict(n=n, m=m, merge_items=s)
+
+
+class ClockSampler:
+    def __init__(self):
+        self.rows, self.proc = [], None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm = sorted(float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit())
+        mx = max((float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()), default=None)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_gbs():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample_run(threads=None):
+    """The CPU path on the bounded sample: T = convert's "process graph" + initial
+    partition + initial WCC + sum of iteration timers (the reference's own timers)."""
+    import oracle
+    import scdgen
+    pairs = scdgen.rmat(CPU_SAMPLE_SCALE, 16, 0.57, 0.19, 0.19, seed=22)
+    ref_bin = os.path.join(ROOT, "oracle", "_ref")
+    g, tm = oracle.convert(pairs)
+    r = oracle.run(g, max_iters=1000, keep_trace=False)
+    t_ms = tm["process_graph"] + r["times"]["initial_partition"] + r["times"]["initial_wcc"] + r["times"]["iterations"]
+    return pairs.shape[0] / (t_ms / 1e3), t_ms, pairs.shape[0], "port"
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    cores = oracle.threads()
+    W, K = args.warmup, args.steps
+    vals = []
+    for i in range(W + K):
+        v, t_ms, e, kind = cpu_sample_run()
+        if i >= W:
+            vals.append((v, t_ms))
+    v = sorted(x[0] for x in vals)[len(vals) // 2]
+    ms = sorted(x[1] for x in vals)[len(vals) // 2]
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": K, "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
+            "config": {"workload": f"rmat-{CPU_SAMPLE_SCALE} sample of rmat-22 (edge factor 16, a/b/c/d .57/.19/.19/.05)",
+                       "edges_in": e, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"R-MAT scale {CPU_SAMPLE_SCALE} (same generator and a,b,c,d), "
+                                       "reference timers: process graph + initial partition + initial WCC + iterations"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine")
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    import scd_gb300 as S
+    import scdgen
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    t0 = time.time()
+    pairs = scdgen.rmat(args.scale, 16, 0.57, 0.19, 0.19, seed=22)
+    gen_s = time.time() - t0
+    E = pairs.shape[0]
+    dev_pairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    host_pairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
+
+    eng = S.Engine(local, flags=S.FLAG_PROFILE)
+    stream = torch.cuda.ExternalStream(eng.stream())
+
+    def step_device():
+        eng.convert_edges(device_ptr=dev_pairs.data_ptr(), count=E)
+        return eng.run(0.01, 1000)
+
+    def step_e2e():
+        rc = S.lib().scd_convert_edges(eng._ctx, host_pairs.data_ptr(), E, 0)
+        eng._check(rc)
+        r = eng.run(0.01, 1000)
+        lab = eng.labels_from_device()
+        return r, lab
+
+    for _ in range(args.warmup):
+        r = step_device()
+    torch.cuda.synchronize()
+    eng.profile_reset()
+    launches0 = eng.kernel_launches()
+    clocks = ClockSampler()
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r = step_device()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    dev_ms = ev0.elapsed_time(ev1) / args.steps
+    launches = eng.kernel_launches() - launches0
+    prof = {p: eng.profile(p) for p in S.PHASES}
+    ck = clocks.stop()
+    # e2e through the public API with host buffers
+    for _ in range(1):
+        step_e2e()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    e_ev0, e_ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_ev0.record(stream)
+    for _ in range(args.steps):
+        r2, lab = step_e2e()
+    e_ev1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t) * 1e3 / args.steps
+    n, m, cc = eng.graph_info()
+
+    if dist:
+        tt = torch.tensor([dev_ms, e2e_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms, e2e_ms = tt.tolist()
+
+    # roofline of the dominant kernel: preprocessing triangle counting
+    gd = eng.graph_download()
+    b_tc, tcinfo = algorithmic_tc_bytes(gd["indices"], gd["adj"])
+    tc_ms, tc_n = prof["tc"]
+    tc_avg = tc_ms / max(tc_n, 1)
+    peak, peak_kind = measured_peak_gbs()
+    achieved = b_tc / (tc_avg / 1e3) / 1e9
+
+    line = {"metric": METRIC, "value": world * E / (dev_ms / 1e3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
+            "config": {"workload": f"rmat-{args.scale}", "edge_factor": 16, "abcd": [0.57, 0.19, 0.19, 0.05],
+                       "edges_in": E, "n": n, "m": m, "iterations": r["iterations"], "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (edge list %d MB)" % (E * 8 >> 20)},
+            "e2e": {"value": world * E / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": E * 8,
+                    "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1)},
+            "gpu_launches": launches,
+            "phases_ms": {p: round(v[0] / max(args.steps, 1), 3) for p, v in prof.items()},
+            "roofline": {"kernel": "k_tc_units (preprocessing triangle counting)", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "algorithmic_bytes": b_tc, "ms_per_launch": tc_avg,
+                         "traffic": None},
+            "clocks": ck, "generate_s": round(gen_s, 2)}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        v, t_ms, e, kind = cpu_sample_run()
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": oracle.threads(), "kind": kind,
+                                "sample": f"R-MAT scale {CPU_SAMPLE_SCALE} ({e} edges), same generator; "
+                                          f"{t_ms:.0f} ms of reference-timer CPU work"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

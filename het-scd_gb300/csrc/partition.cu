@@ -1,0 +1,171 @@
+// Initial partition on the device (create_initial_partition,
+// src/scd.cpp:113-171).
+//
+// The reference sorts vertices by ((cc, deg), id) descending and walks them
+// sequentially: a still-unlabelled vertex opens the next label and claims its
+// unlabelled neighbours.  Exact parallel form used here: a vertex is a seed iff
+// no neighbour earlier in the order is a seed (the lexicographically-first
+// maximal independent set of that order); a seed's label is its rank among the
+// seeds; a non-seed takes the label of its earliest seed neighbour (that seed
+// reached it first).  The order comes from two stable LSD radix sorts:
+// (deg, id) then the cc bits (positive doubles order like their bit patterns).
+// The independent set is found in rounds: an undecided vertex becomes a
+// non-seed as soon as an earlier neighbour is a seed, and a seed once every
+// earlier neighbour is a decided non-seed.
+#include "engine.cuh"
+
+namespace scd {
+
+namespace {
+
+constexpr unsigned TPB = 256;
+constexpr uint8_t UNDECIDED = 0, SEED = 1, NONSEED = 2;
+
+__global__ void k_order_keys(uint32_t n, const uint32_t *__restrict__ indices, uint64_t *keys, uint32_t *vals) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t d = indices[v + 1] - indices[v];
+        keys[v] = ((uint64_t)(0xffffffffu - d) << 32) | (0xffffffffu - v);
+        vals[v] = v;
+    }
+}
+
+// cc = tri / (deg * (deg - 1.0)) (src/scd.cpp:129-131); key = ~bits so that
+// ascending order is cc descending
+__global__ void k_cc_keys(uint32_t n, const uint32_t *__restrict__ order, const uint32_t *__restrict__ indices,
+                          const int32_t *__restrict__ tri, uint64_t *keys) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t v = order[i];
+        const uint32_t d = indices[v + 1] - indices[v];
+        const double cc = __ddiv_rn((double)tri[v], __dmul_rn((double)d, __dsub_rn((double)d, 1.0)));
+        keys[i] = ~(uint64_t)__double_as_longlong(cc);
+    }
+}
+
+__global__ void k_positions(uint32_t n, const uint32_t *__restrict__ order, uint32_t *pos) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[order[i]] = i;
+}
+
+__global__ void __launch_bounds__(TPB)
+k_mis_round(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
+            const uint32_t *__restrict__ pos, uint8_t *state, uint32_t *undecided) {
+    const int lane = threadIdx.x & 31;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += (gridDim.x * blockDim.x) >> 5) {
+        if (((volatile uint8_t *)state)[v] != UNDECIDED) continue;
+        const uint32_t pv = pos[v], beg = indices[v], deg = indices[v + 1] - beg;
+        bool seed_seen = false, open = false;
+        for (uint32_t i0 = 0; i0 < deg && !seed_seen; i0 += 32) {
+            bool s = false, u = false;
+            if (i0 + lane < deg) {
+                const uint32_t w = adj[beg + i0 + lane];
+                if (pos[w] < pv) {
+                    const uint8_t st = ((volatile uint8_t *)state)[w];
+                    s = st == SEED;
+                    u = st == UNDECIDED;
+                }
+            }
+            seed_seen = __any_sync(FULL, s);
+            open = open || __any_sync(FULL, u);
+        }
+        if (lane == 0) {
+            if (seed_seen) state[v] = NONSEED;
+            else if (!open) state[v] = SEED;
+            else atomicAdd(undecided, 1u);
+        }
+    }
+}
+
+struct SeedAt {
+    const uint32_t *order;
+    const uint8_t *state;
+    __device__ uint32_t operator[](size_t i) const { return state[order[i]] == SEED; }
+};
+
+__global__ void k_seed_labels(uint32_t n, const uint32_t *__restrict__ pos, const uint8_t *__restrict__ state,
+                              const uint32_t *__restrict__ seed_rank, uint32_t *labels) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        if (state[v] == SEED) labels[v] = seed_rank[pos[v]];
+}
+
+__global__ void __launch_bounds__(TPB)
+k_claim_labels(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
+               const uint32_t *__restrict__ pos, const uint8_t *__restrict__ state, uint32_t *labels) {
+    const int lane = threadIdx.x & 31;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += (gridDim.x * blockDim.x) >> 5) {
+        if (state[v] != NONSEED) continue;
+        const uint32_t beg = indices[v], deg = indices[v + 1] - beg;
+        uint32_t best_pos = INVALID, best = INVALID;
+        for (uint32_t i = lane; i < deg; i += 32) {
+            const uint32_t w = adj[beg + i];
+            if (state[w] == SEED && pos[w] < best_pos) {
+                best_pos = pos[w];
+                best = w;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            uint32_t op = __shfl_xor_sync(FULL, best_pos, o), ob = __shfl_xor_sync(FULL, best, o);
+            if (op < best_pos) {
+                best_pos = op;
+                best = ob;
+            }
+        }
+        if (lane == 0) labels[v] = labels[best];
+    }
+}
+
+}  // namespace
+
+void initial_partition(Ctx &c) {
+    const Graph &g = c.g;
+    cudaStream_t s = c.stream;
+    const uint32_t n = g.n;
+    c.num_comms = 0;
+    if (n == 0) {
+        c.has_labels = true;
+        return;
+    }
+    PhaseScope ph(c, "partition");
+    DevBuf<uint64_t> keys(n, s);
+    DevBuf<uint32_t> order(n, s), pos(n, s), undecided(1, s);
+    k_order_keys<<<grid_for(n, TPB), TPB, 0, s>>>(n, g.indices, keys.get(), order.get());
+    CK_LAUNCH("k_order_keys");
+    radix_sort<uint64_t>(keys.get(), order.get(), n, 0, 64, s);
+    k_cc_keys<<<grid_for(n, TPB), TPB, 0, s>>>(n, order.get(), g.indices, g.tri, keys.get());
+    CK_LAUNCH("k_cc_keys");
+    radix_sort<uint64_t>(keys.get(), order.get(), n, 0, 64, s);
+    keys.release();
+    k_positions<<<grid_for(n, TPB), TPB, 0, s>>>(n, order.get(), pos.get());
+    CK_LAUNCH("k_positions");
+    c.launches += 3;
+
+    DevBuf<uint8_t> state(n, s);
+    CK(cudaMemsetAsync(state.get(), UNDECIDED, n, s));
+    const unsigned G = grid_for((uint64_t)n * 32, TPB);
+    for (int round = 0;; round++) {
+        CK(cudaMemsetAsync(undecided.get(), 0, 4, s));
+        k_mis_round<<<G, TPB, 0, s>>>(n, g.indices, g.adj, pos.get(), state.get(), undecided.get());
+        CK_LAUNCH("k_mis_round");
+        c.launches++;
+        uint32_t left = 0;
+        CK(cudaMemcpyAsync(&left, undecided.get(), 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (left == 0) break;
+        if (round > 4 * (int)n + 8) throw Error(SCD_ERR_TIMEOUT, "initial partition did not converge");
+    }
+
+    DevBuf<uint32_t> rank((size_t)n + 1, s);
+    scan_exclusive<uint32_t>(SeedAt{order.get(), state.get()}, rank.get(), n, s);
+    k_seed_labels<<<grid_for(n, TPB), TPB, 0, s>>>(n, pos.get(), state.get(), rank.get(), c.labels);
+    CK_LAUNCH("k_seed_labels");
+    k_claim_labels<<<G, TPB, 0, s>>>(n, g.indices, g.adj, pos.get(), state.get(), c.labels);
+    CK_LAUNCH("k_claim_labels");
+    c.launches += 4;
+    CK(cudaMemcpyAsync(&c.num_comms, rank.get() + n, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    c.cur = 0;
+    collect_stats(c, c.labels, c.st[0]);
+    CK(cudaMemcpyAsync(c.best, c.labels, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    c.has_labels = true;
+}
+
+}  // namespace scd

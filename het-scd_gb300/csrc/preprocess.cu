@@ -1,0 +1,373 @@
+// Preprocessing on the device: the work of the reference's `convert` tool
+// (src/convert.cpp:141-463), which the reference runs on the CPU only.
+//
+//  1. first-appearance renumbering (src/convert.cpp:141-170): first position of
+//     every raw id (atomicMin over the 2E endpoint slots), a bitmap of those
+//     positions and a popcount prefix give each id its rank of first appearance;
+//  2. both directions of every renamed non-loop pair as one 2k-bit key
+//     (row << k | col), one stable LSD radix sort, adjacent duplicates dropped:
+//     the de-duplicated symmetric CSR (src/convert.cpp:252-268 + 417-463);
+//  3. degree orientation (u -> v iff (deg v, v) > (deg u, u)) and per-out-slot
+//     triangle counts (triangles.cu); per vertex tri = sum of counts, tri_deg =
+//     number of edges with a count > 0 (src/convert.cpp:271-340);
+//  4. triangle-free edges dropped and vertices ranked by (tri_deg, id)
+//     descending, degree-0 vertices trimmed (src/convert.cpp:342-414);
+//  5. the final symmetric CSR by a second key sort (src/convert.cpp:417-455).
+#include "engine.cuh"
+
+namespace scd {
+
+namespace {
+
+constexpr unsigned TPB = 256;
+
+__global__ void k_first_pos(const uint32_t *__restrict__ pairs, uint64_t count, uint32_t *first) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t a = pairs[2 * i], b = pairs[2 * i + 1];
+        uint32_t pa = (uint32_t)(2 * i), pb = pa + 1;
+        if (first[a] > pa) atomicMin(first + a, pa);
+        if (first[b] > pb) atomicMin(first + b, pb);
+    }
+}
+
+__global__ void k_mark_first(const uint32_t *__restrict__ first, uint32_t n_raw, uint32_t *bits) {
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n_raw; x += gridDim.x * blockDim.x) {
+        uint32_t p = first[x];
+        if (p != INVALID) atomicOr(bits + (p >> 5), 1u << (p & 31));
+    }
+}
+
+struct PopcountOf {
+    const uint32_t *bits;
+    __device__ uint32_t operator[](size_t i) const { return __popc(bits[i]); }
+};
+
+// first[x] (position of first appearance) -> new id (rank of that position)
+__global__ void k_rename(uint32_t *first, uint32_t n_raw, const uint32_t *__restrict__ bits,
+                         const uint32_t *__restrict__ word_prefix) {
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n_raw; x += gridDim.x * blockDim.x) {
+        uint32_t p = first[x];
+        if (p != INVALID) {
+            uint32_t w = p >> 5, b = p & 31;
+            first[x] = word_prefix[w] + __popc(bits[w] & ((1u << b) - 1u));
+        }
+    }
+}
+
+__global__ void k_directed_keys(const uint32_t *__restrict__ pairs, uint64_t count,
+                                const uint32_t *__restrict__ rename, int k, uint64_t *keys) {
+    const uint64_t sentinel = ~0ull >> (64 - 2 * k);
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t a = rename[pairs[2 * i]], b = rename[pairs[2 * i + 1]];
+        if (a != b) {
+            keys[2 * i] = (a << k) | b;
+            keys[2 * i + 1] = (b << k) | a;
+        } else {
+            keys[2 * i] = sentinel;
+            keys[2 * i + 1] = sentinel;
+        }
+    }
+}
+
+struct FirstOfRun {
+    const uint64_t *keys;
+    uint64_t sentinel;
+    __device__ uint32_t operator[](size_t i) const {
+        uint64_t k = keys[i];
+        return k != sentinel && (i == 0 || keys[i - 1] != k);
+    }
+};
+
+__global__ void k_compact_keys(const uint64_t *__restrict__ keys, uint64_t count, uint64_t sentinel,
+                               const uint32_t *__restrict__ pos, int k, uint32_t *rows, uint32_t *cols) {
+    const uint64_t mask = (1ull << k) - 1;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t key = keys[i];
+        if (key != sentinel && (i == 0 || keys[i - 1] != key)) {
+            uint32_t o = pos[i];
+            rows[o] = (uint32_t)(key >> k);
+            cols[o] = (uint32_t)(key & mask);
+        }
+    }
+}
+
+// row offsets of a row-sorted COO list: indices[r] = first slot of row >= r
+__global__ void k_row_offsets(const uint32_t *__restrict__ rows, uint32_t count, uint32_t n_rows,
+                              uint32_t *indices) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= count; i += gridDim.x * blockDim.x) {
+        uint32_t hi = i < count ? rows[i] : n_rows;
+        int64_t lo = i == 0 ? -1 : (int64_t)rows[i - 1];
+        for (int64_t r = lo + 1; r <= (int64_t)hi && r <= (int64_t)n_rows; r++) indices[r] = i;
+    }
+}
+
+struct IsOut {
+    const uint32_t *rows, *cols, *indices;
+    __device__ uint32_t operator[](size_t i) const {
+        uint32_t u = rows[i], v = cols[i];
+        uint32_t du = indices[u + 1] - indices[u], dv = indices[v + 1] - indices[v];
+        return dv > du || (dv == du && v > u);
+    }
+};
+
+__global__ void k_orient(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
+                         const uint32_t *__restrict__ indices, uint32_t count,
+                         const uint32_t *__restrict__ pos, uint32_t *orow, uint32_t *ocol) {
+    IsOut f{rows, cols, indices};
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        if (f[i]) {
+            orow[pos[i]] = rows[i];
+            ocol[pos[i]] = cols[i];
+        }
+    }
+}
+
+__global__ void k_out_ranges(const uint32_t *__restrict__ indices, const uint32_t *__restrict__ pos,
+                             uint32_t n, uint32_t *obeg, uint32_t *olen) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+        uint32_t b = pos[indices[u]], e = pos[indices[u + 1]];
+        obeg[u] = b;
+        olen[u] = e - b;
+    }
+}
+
+// tri[v] = sum of the counts of v's edges, tri_deg[v] = edges with count > 0
+// (src/convert.cpp:327-340; int32 wrap-around as in the reference)
+__global__ void k_vertex_triangles(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
+                                   const uint32_t *__restrict__ cnt, uint32_t count, int32_t *tri,
+                                   int32_t *tri_deg) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        uint32_t c = cnt[i];
+        if (c > 0) {
+            uint32_t u = orow[i], v = ocol[i];
+            atomicAdd((uint32_t *)tri + u, c);
+            atomicAdd((uint32_t *)tri + v, c);
+            atomicAdd(tri_deg + u, 1);
+            atomicAdd(tri_deg + v, 1);
+        }
+    }
+}
+
+// key = ((2^32-1 - tri_deg) << k) | (2^k-1 - v): ascending = (tri_deg, v) descending
+__global__ void k_degree_keys(const int32_t *__restrict__ tri_deg, uint32_t n, int k, uint64_t *keys,
+                              uint32_t *vals) {
+    const uint64_t vmax = (1ull << k) - 1;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        keys[v] = ((uint64_t)(0xffffffffu - (uint32_t)tri_deg[v]) << k) | (vmax - v);
+        vals[v] = v;
+    }
+}
+
+__global__ void k_rank_of(const uint32_t *__restrict__ order, uint32_t n, const int32_t *__restrict__ tri,
+                          const int32_t *__restrict__ tri_deg, uint32_t *rank, int32_t *tri_out,
+                          int32_t *tri_deg_out, uint32_t n_keep) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        uint32_t v = order[r];
+        rank[v] = r;
+        if (r < n_keep) {
+            tri_out[r] = tri[v];
+            tri_deg_out[r] = tri_deg[v];
+        }
+    }
+}
+
+struct Positive {
+    const uint32_t *cnt;
+    __device__ uint32_t operator[](size_t i) const { return cnt[i] > 0; }
+};
+
+struct NonZeroDeg {
+    const int32_t *d;
+    __device__ uint32_t operator[](size_t i) const { return d[i] > 0; }
+};
+
+__global__ void k_final_keys(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
+                             const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pos,
+                             uint32_t count, const uint32_t *__restrict__ rank, int k, uint64_t *keys) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        if (cnt[i] > 0) {
+            uint64_t a = rank[orow[i]], b = rank[ocol[i]];
+            uint32_t o = pos[i];
+            keys[2 * (uint64_t)o] = (a << k) | b;
+            keys[2 * (uint64_t)o + 1] = (b << k) | a;
+        }
+    }
+}
+
+__global__ void k_split_keys(const uint64_t *__restrict__ keys, uint32_t count, int k, uint32_t *rows,
+                             uint32_t *cols) {
+    const uint64_t mask = (1ull << k) - 1;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        rows[i] = (uint32_t)(keys[i] >> k);
+        cols[i] = (uint32_t)(keys[i] & mask);
+    }
+}
+
+template <typename T>
+T read_scalar(const T *dev, cudaStream_t s) {
+    T h;
+    CK(cudaMemcpyAsync(&h, dev, sizeof(T), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return h;
+}
+
+}  // namespace
+
+void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
+    cudaStream_t s = c.stream;
+    if (count >= (1ull << 31)) throw Error(SCD_ERR_LIMIT, "more than 2^31-1 edge records");
+    c.free_all();
+    if (count == 0) {
+        upload_graph(c, 0, 0, nullptr, nullptr, nullptr, nullptr);
+        return;
+    }
+    PhaseScope ph(c, "convert");
+    const unsigned G = grid_for(count, TPB, 152 * 32);
+
+    // 1. first-appearance renumbering
+    DevBuf<uint32_t> mx(1, s);
+    CK(cudaMemsetAsync(mx.get(), 0, 4, s));
+    k_reduce_max<uint32_t><<<grid_for(2 * count, TPB, 152 * 16), TPB, 0, s>>>(pairs, 2 * count, mx.get());
+    CK_LAUNCH("k_reduce_max");
+    const uint32_t n_raw = read_scalar(mx.get(), s) + 1;
+    if (n_raw == 0) throw Error(SCD_ERR_LIMIT, "vertex id 2^32-1 is not supported");
+    DevBuf<uint32_t> rename(n_raw, s);
+    CK(cudaMemsetAsync(rename.get(), 0xff, (size_t)n_raw * 4, s));
+    k_first_pos<<<G, TPB, 0, s>>>(pairs, count, rename.get());
+    CK_LAUNCH("k_first_pos");
+    const size_t words = (2 * count + 31) / 32;
+    DevBuf<uint32_t> bits(words, s), wpre(words + 1, s);
+    CK(cudaMemsetAsync(bits.get(), 0, words * 4, s));
+    k_mark_first<<<grid_for(n_raw, TPB), TPB, 0, s>>>(rename.get(), n_raw, bits.get());
+    CK_LAUNCH("k_mark_first");
+    scan_exclusive<uint32_t>(PopcountOf{bits.get()}, wpre.get(), words, s);
+    k_rename<<<grid_for(n_raw, TPB), TPB, 0, s>>>(rename.get(), n_raw, bits.get(), wpre.get());
+    CK_LAUNCH("k_rename");
+    const uint32_t n1 = read_scalar(wpre.get() + words, s);
+    bits.release();
+    wpre.release();
+
+    // 2. de-duplicated symmetric CSR over the renamed ids
+    const int k1 = ceil_log2(n1 < 2 ? 2 : n1);
+    const uint64_t sent1 = ~0ull >> (64 - 2 * k1);
+    DevBuf<uint64_t> keys(2 * count, s);
+    k_directed_keys<<<G, TPB, 0, s>>>(pairs, count, rename.get(), k1, keys.get());
+    CK_LAUNCH("k_directed_keys");
+    rename.release();
+    radix_sort<uint64_t>(keys.get(), nullptr, 2 * count, 0, 2 * k1, s);
+    DevBuf<uint32_t> kpos(2 * count + 1, s);
+    scan_exclusive<uint32_t>(FirstOfRun{keys.get(), sent1}, kpos.get(), 2 * count, s);
+    const uint32_t slots1 = read_scalar(kpos.get() + 2 * count, s);
+    DevBuf<uint32_t> rows1(slots1, s), cols1(slots1, s), ind1(n1 + 1, s);
+    k_compact_keys<<<grid_for(2 * count, TPB), TPB, 0, s>>>(keys.get(), 2 * count, sent1, kpos.get(), k1,
+                                                           rows1.get(), cols1.get());
+    CK_LAUNCH("k_compact_keys");
+    keys.release();
+    kpos.release();
+    k_row_offsets<<<grid_for(slots1 + 1, TPB), TPB, 0, s>>>(rows1.get(), slots1, n1, ind1.get());
+    CK_LAUNCH("k_row_offsets");
+    const uint32_t m1 = slots1 / 2;
+
+    // 3. degree orientation + triangle counts
+    DevBuf<uint32_t> opos(slots1 + 1, s);
+    scan_exclusive<uint32_t>(IsOut{rows1.get(), cols1.get(), ind1.get()}, opos.get(), slots1, s);
+    DevBuf<uint32_t> orow(m1, s), ocol(m1, s), obeg(n1, s), olen(n1, s), ocnt(m1, s);
+    k_orient<<<grid_for(slots1, TPB), TPB, 0, s>>>(rows1.get(), cols1.get(), ind1.get(), slots1, opos.get(),
+                                                  orow.get(), ocol.get());
+    CK_LAUNCH("k_orient");
+    k_out_ranges<<<grid_for(n1, TPB), TPB, 0, s>>>(ind1.get(), opos.get(), n1, obeg.get(), olen.get());
+    CK_LAUNCH("k_out_ranges");
+    opos.release();
+    rows1.release();
+    cols1.release();
+    ind1.release();
+    CK(cudaMemsetAsync(ocnt.get(), 0, (size_t)m1 * 4, s));
+    Oriented o{obeg.get(), olen.get(), ocol.get(), n1};
+    count_oriented_triangles(c, o, nullptr, ocnt.get(), s);
+    DevBuf<int32_t> tri1(n1, s), tdeg1(n1, s);
+    CK(cudaMemsetAsync(tri1.get(), 0, (size_t)n1 * 4, s));
+    CK(cudaMemsetAsync(tdeg1.get(), 0, (size_t)n1 * 4, s));
+    k_vertex_triangles<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), ocnt.get(), m1, tri1.get(),
+                                                        tdeg1.get());
+    CK_LAUNCH("k_vertex_triangles");
+    obeg.release();
+    olen.release();
+
+    // 4. rank by (tri_deg, id) descending; trim vertices without triangle edges
+    DevBuf<uint32_t> nkeep(2, s);
+    {
+        DevBuf<uint32_t> tmp(n1 + 1, s);
+        scan_exclusive<uint32_t>(NonZeroDeg{tdeg1.get()}, tmp.get(), n1, s);
+        CK(cudaMemcpyAsync(nkeep.get(), tmp.get() + n1, 4, cudaMemcpyDeviceToDevice, s));
+    }
+    const uint32_t n2 = read_scalar(nkeep.get(), s);
+    DevBuf<uint64_t> dkeys(n1, s);
+    DevBuf<uint32_t> order(n1, s), rank(n1, s);
+    k_degree_keys<<<grid_for(n1, TPB), TPB, 0, s>>>(tdeg1.get(), n1, k1, dkeys.get(), order.get());
+    CK_LAUNCH("k_degree_keys");
+    radix_sort<uint64_t>(dkeys.get(), order.get(), n1, 0, 32 + k1, s);
+    dkeys.release();
+
+    // 5. final symmetric CSR in rank ids
+    DevBuf<uint32_t> fpos(m1 + 1, s);
+    scan_exclusive<uint32_t>(Positive{ocnt.get()}, fpos.get(), m1, s);
+    const uint32_t m2 = read_scalar(fpos.get() + m1, s);
+
+    Graph &g = c.g;
+    g.n = n2;
+    g.m = m2;
+    g.indices = c.alloc<uint32_t>((size_t)n2 + 1);
+    g.adj = c.alloc<uint32_t>(2 * (size_t)m2);
+    g.tri = c.alloc<int32_t>(n2);
+    g.tri_deg = c.alloc<int32_t>(n2);
+    k_rank_of<<<grid_for(n1, TPB), TPB, 0, s>>>(order.get(), n1, tri1.get(), tdeg1.get(), rank.get(), g.tri,
+                                               g.tri_deg, n2);
+    CK_LAUNCH("k_rank_of");
+    if (m2 > 0) {
+        const int k2 = ceil_log2(n2 < 2 ? 2 : n2);
+        DevBuf<uint64_t> fkeys(2 * (size_t)m2, s);
+        k_final_keys<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), ocnt.get(), fpos.get(), m1,
+                                                      rank.get(), k2, fkeys.get());
+        CK_LAUNCH("k_final_keys");
+        radix_sort<uint64_t>(fkeys.get(), nullptr, 2 * (size_t)m2, 0, 2 * k2, s);
+        DevBuf<uint32_t> frows(2 * (size_t)m2, s);
+        k_split_keys<<<grid_for(2 * (size_t)m2, TPB), TPB, 0, s>>>(fkeys.get(), 2 * m2, k2, frows.get(), g.adj);
+        CK_LAUNCH("k_split_keys");
+        k_row_offsets<<<grid_for(2 * (size_t)m2 + 1, TPB), TPB, 0, s>>>(frows.get(), 2 * m2, n2, g.indices);
+        CK_LAUNCH("k_row_offsets");
+    } else {
+        CK(cudaMemsetAsync(g.indices, 0, ((size_t)n2 + 1) * 4, s));
+    }
+    c.has_graph = true;
+    finish_graph(c);
+}
+
+void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
+                  const int32_t *tri, const int32_t *tri_deg) {
+    cudaStream_t s = c.stream;
+    c.free_all();
+    Graph &g = c.g;
+    g.n = n;
+    g.m = m;
+    g.indices = c.alloc<uint32_t>((size_t)n + 1);
+    g.adj = c.alloc<uint32_t>(2 * (size_t)m);
+    g.tri = c.alloc<int32_t>(n);
+    g.tri_deg = c.alloc<int32_t>(n);
+    if (indices) {
+        CK(cudaMemcpyAsync(g.indices, indices, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice, s));
+        if (m) CK(cudaMemcpyAsync(g.adj, adj, 2 * (size_t)m * 4, cudaMemcpyHostToDevice, s));
+        if (n) {
+            CK(cudaMemcpyAsync(g.tri, tri, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+            CK(cudaMemcpyAsync(g.tri_deg, tri_deg, (size_t)n * 4, cudaMemcpyHostToDevice, s));
+        }
+    } else {
+        CK(cudaMemsetAsync(g.indices, 0, ((size_t)n + 1) * 4, s));
+    }
+    c.has_graph = true;
+    finish_graph(c);
+}
+
+}  // namespace scd

@@ -1,0 +1,228 @@
+"""Python binding of the C ABI in include/scd_gb300.h (libscd_gb300.so).
+
+Mirrors the reference's GPU backend interface (src/cuda.hpp:23-28) one call per
+function, plus the device-side preprocessing of `convert` and the full run
+loop.  Every call goes straight to the CUDA library; there is no CPU path, and
+constructing an Engine fails loudly when the library or a GPU is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libscd_gb300.so")
+HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "scd_gb300.h")
+_LIB = None
+
+OK = 0
+ERRORS = {-1: "SCD_ERR_ARG", -2: "SCD_ERR_CUDA", -3: "SCD_ERR_OOM", -4: "SCD_ERR_STATE",
+          -5: "SCD_ERR_FORMAT", -6: "SCD_ERR_TIMEOUT", -7: "SCD_ERR_LIMIT"}
+INVALID_LABEL = 0xFFFFFFFF
+FLAG_PROFILE, FLAG_PEXT_TREE = 1, 2
+PHASES = ("convert", "tc", "partition", "improve", "stats", "wcc_tc", "wcc")
+
+
+class ScdError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{ERRORS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("initial_wcc", ctypes.c_double),
+                ("best_wcc", ctypes.c_double), ("initial_communities", ctypes.c_uint32),
+                ("printed_communities", ctypes.c_uint32), ("distinct_communities", ctypes.c_uint32),
+                ("ms_partition", ctypes.c_double), ("ms_iterations", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: the CUDA engine was not built "
+                               "(run __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        u32, u64, i32, dbl = ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int, ctypes.c_double
+        sig = {
+            "scd_create": ([ctypes.POINTER(P), i32, i32, ctypes.c_uint], i32),
+            "scd_destroy": ([P], None),
+            "scd_last_error": ([P], ctypes.c_char_p),
+            "scd_convert_edges": ([P, P, u64, i32], i32),
+            "scd_transfer_graph": ([P, u32, u32, P, P, P, P, dbl], i32),
+            "scd_graph_info": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(dbl)], i32),
+            "scd_graph_download": ([P, P, P, P, P], i32),
+            "scd_initial_partition": ([P, ctypes.POINTER(u32)], i32),
+            "scd_labels_to_device": ([P, P], i32),
+            "scd_compute_wcc": ([P, ctypes.POINTER(dbl)], i32),
+            "scd_improve_labels": ([P, ctypes.POINTER(dbl)], i32),
+            "scd_store_labels": ([P], i32),
+            "scd_labels_from_device": ([P, P], i32),
+            "scd_current_labels": ([P, P], i32),
+            "scd_community_stats": ([P, P, P, P, ctypes.POINTER(u32)], i32),
+            "scd_run": ([P, dbl, i32, P, ctypes.POINTER(Result)], i32),
+            "scd_memory_usage": ([P, ctypes.POINTER(u64)], i32),
+            "scd_kernel_launches": ([P, ctypes.POINTER(u64)], i32),
+            "scd_stream": ([P, ctypes.POINTER(P)], i32),
+            "scd_profile_get": ([P, ctypes.c_char_p, ctypes.POINTER(dbl), ctypes.POINTER(u64)], i32),
+            "scd_profile_reset": ([P], i32),
+        }
+        for name, (args, res) in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+def header_symbols():
+    """Names of the functions include/scd_gb300.h declares."""
+    import re
+    text = open(HEADER_PATH).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(scd_\w+)\s*\(", text, re.M)))
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+class Engine:
+    """One SCD context (one graph) on one GPU."""
+
+    def __init__(self, device=0, work_group_size=256, flags=0):
+        self._ctx = ctypes.c_void_p()
+        rc = lib().scd_create(ctypes.byref(self._ctx), device, work_group_size, flags)
+        if rc != OK:
+            raise ScdError(rc, f"cannot open CUDA device {device}")
+
+    def _check(self, rc):
+        if rc != OK:
+            raise ScdError(rc, lib().scd_last_error(self._ctx).decode())
+
+    def close(self):
+        if self._ctx:
+            lib().scd_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- graph -------------------------------------------------------------
+    def convert_edges(self, pairs=None, device_ptr=None, count=None):
+        """Device preprocessing (convert) of (min,max) pairs in file order."""
+        if device_ptr is not None:
+            self._check(lib().scd_convert_edges(self._ctx, device_ptr, count, 1))
+            return
+        pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
+        self._check(lib().scd_convert_edges(self._ctx, _p(pairs), pairs.shape[0], 0))
+
+    def transfer_graph(self, g, alpha=1.0):
+        arrs = [np.ascontiguousarray(getattr(g, k), dtype=t) for k, t in
+                (("indices", np.uint32), ("adj", np.uint32), ("tri", np.int32), ("tri_deg", np.int32))]
+        self._check(lib().scd_transfer_graph(self._ctx, g.n, g.m, *[_p(a) for a in arrs], alpha))
+
+    def graph_info(self):
+        n, m, cc = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
+        self._check(lib().scd_graph_info(self._ctx, ctypes.byref(n), ctypes.byref(m), ctypes.byref(cc)))
+        return n.value, m.value, cc.value
+
+    def graph_download(self):
+        n, m, _ = self.graph_info()
+        ind = np.empty(n + 1, np.uint32)
+        adj = np.empty(2 * m, np.uint32)
+        tri = np.empty(n, np.int32)
+        tdg = np.empty(n, np.int32)
+        self._check(lib().scd_graph_download(self._ctx, _p(ind), _p(adj), _p(tri), _p(tdg)))
+        return dict(n=n, m=m, indices=ind, adj=adj, tri=tri, tri_deg=tdg)
+
+    def graph_bytes(self):
+        d = self.graph_download()
+        hdr = np.array([d["n"], d["m"]], np.uint32)
+        return b"".join(a.tobytes() for a in (hdr, d["indices"], d["adj"], d["tri"], d["tri_deg"]))
+
+    # --- partition ----------------------------------------------------------
+    def initial_partition(self):
+        nc = ctypes.c_uint32()
+        self._check(lib().scd_initial_partition(self._ctx, ctypes.byref(nc)))
+        return nc.value
+
+    def labels_to_device(self, labels):
+        labels = np.ascontiguousarray(labels, dtype=np.uint32)
+        self._check(lib().scd_labels_to_device(self._ctx, _p(labels)))
+
+    def compute_wcc(self):
+        w = ctypes.c_double()
+        self._check(lib().scd_compute_wcc(self._ctx, ctypes.byref(w)))
+        return w.value
+
+    def improve_labels(self):
+        w = ctypes.c_double()
+        self._check(lib().scd_improve_labels(self._ctx, ctypes.byref(w)))
+        return w.value
+
+    def store_labels(self):
+        self._check(lib().scd_store_labels(self._ctx))
+
+    def labels_from_device(self):
+        n = self.graph_info()[0]
+        out = np.empty(n, np.uint32)
+        self._check(lib().scd_labels_from_device(self._ctx, _p(out)))
+        return out
+
+    def current_labels(self):
+        n = self.graph_info()[0]
+        out = np.empty(n, np.uint32)
+        self._check(lib().scd_current_labels(self._ctx, _p(out)))
+        return out
+
+    def community_stats(self):
+        nc = ctypes.c_uint32()
+        self._check(lib().scd_community_stats(self._ctx, None, None, None, ctypes.byref(nc)))
+        k = nc.value
+        s, e, i = (np.empty(max(k, 1), np.int32) for _ in range(3))
+        self._check(lib().scd_community_stats(self._ctx, _p(s), _p(e), _p(i), ctypes.byref(nc)))
+        return s[:k], e[:k], i[:k]
+
+    def run(self, threshold=0.01, max_iters=1000):
+        trace = np.zeros(max_iters, np.float64)
+        r = Result()
+        self._check(lib().scd_run(self._ctx, threshold, max_iters, _p(trace), ctypes.byref(r)))
+        d = r.as_dict()
+        d["wcc"] = trace[: r.iterations].copy()
+        return d
+
+    def memory_usage(self):
+        b = ctypes.c_uint64()
+        self._check(lib().scd_memory_usage(self._ctx, ctypes.byref(b)))
+        return b.value
+
+    def stream(self):
+        p = ctypes.c_void_p()
+        self._check(lib().scd_stream(self._ctx, ctypes.byref(p)))
+        return p.value
+
+    def profile(self, phase):
+        ms, cnt = ctypes.c_double(), ctypes.c_uint64()
+        self._check(lib().scd_profile_get(self._ctx, phase.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
+        return ms.value, cnt.value
+
+    def profile_reset(self):
+        self._check(lib().scd_profile_reset(self._ctx))
+
+    def kernel_launches(self):
+        b = ctypes.c_uint64()
+        self._check(lib().scd_kernel_launches(self._ctx, ctypes.byref(b)))
+        return b.value

@@ -1,0 +1,148 @@
+/*
+ * scd_gb300 — C ABI of the GB300-native SCD engine (libscd_gb300.so).
+ *
+ * Drop-in for the reference's single-GPU backend (src/cuda.hpp:23-28, driven
+ * by src/main-gpu.cpp) plus the preprocessing of the `convert` tool
+ * (src/convert.cpp:141-463), which the reference runs on the CPU only.
+ *
+ * Conventions (differences from the reference are deliberate):
+ *  - every entry point takes an opaque scd_ctx* instead of module globals
+ *    (src/cuda.cu:29-52), so several graphs can live in one process;
+ *  - every entry point returns an int status (SCD_OK or an SCD_ERR_* code)
+ *    instead of calling exit() (src/cuda-common.cuh:67-77); the message of the
+ *    last failure is available from scd_last_error();
+ *  - host buffers are owned by the caller; device memory by the context;
+ *  - one host thread per context; calls on a context are stream-ordered.
+ *  - labels are uint32 with SCD_INVALID_LABEL (src/scd.hpp:23) for "no community".
+ */
+#ifndef SCD_GB300_H
+#define SCD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCD_OK 0
+#define SCD_ERR_ARG (-1)      /* invalid argument                          */
+#define SCD_ERR_CUDA (-2)     /* CUDA runtime error                        */
+#define SCD_ERR_OOM (-3)      /* device allocation failed / over budget    */
+#define SCD_ERR_STATE (-4)    /* call out of order (no graph, no labels)   */
+#define SCD_ERR_FORMAT (-5)   /* malformed graph or edge input             */
+#define SCD_ERR_TIMEOUT (-6)  /* a bounded device-side wait gave up        */
+#define SCD_ERR_LIMIT (-7)    /* input beyond a documented size limit      */
+
+#define SCD_INVALID_LABEL 0xffffffffu
+
+/* scd_create flags */
+#define SCD_FLAG_PROFILE 1u       /* record per-phase CUDA-event timers (scd_profile_get), the
+                                     counterpart of the event timers of src/cuda.cu:351-360 */
+#define SCD_FLAG_PEXT_TREE 2u     /* p_ext by a parallel tree sum instead of the canonical
+                                     index-ordered sum (faster; may differ in the last bits) */
+
+typedef struct scd_ctx scd_ctx;
+
+/* Replaces cuda_init(device_id, work_group_size, profile) (src/cuda.hpp:23,
+ * src/cuda.cu:55-82).  work_group_size is kept for argv compatibility
+ * (src/main-gpu.cpp:38); kernels choose their own launch shapes. */
+int scd_create(scd_ctx **ctx, int device_id, int work_group_size, unsigned flags);
+void scd_destroy(scd_ctx *ctx);
+const char *scd_last_error(const scd_ctx *ctx);
+
+/* Preprocessing on the device: the work of `convert` between reading the text
+ * and writing the file (src/convert.cpp:487-525: first-appearance renumbering,
+ * sort, de-duplication, loop removal, triangle counting, removal of
+ * triangle-free edges, degree relabelling) followed by the symmetric CSR of
+ * write_edges (src/convert.cpp:417-463).  pairs holds count (a, b) records as
+ * read_edges stores them ((min, max) of each text line, in file order,
+ * src/convert.cpp:120-123).  pairs_on_device != 0 means pairs is a device
+ * pointer.  The resulting graph stays resident in the context. */
+int scd_convert_edges(scd_ctx *ctx, const uint32_t *pairs, uint64_t count, int pairs_on_device);
+
+/* Replaces cuda_transfer_graph(const Graph*, alpha) (src/cuda.hpp:24,
+ * src/cuda.cu:84-148): uploads a graph in the binary-format layout
+ * (src/graph.cpp:86-134).  The clustering coefficient p_ext
+ * (src/graph.cpp:57-68) is computed on the device. */
+int scd_transfer_graph(scd_ctx *ctx, uint32_t n, uint32_t m, const uint32_t *indices,
+                       const uint32_t *adj, const int32_t *tri, const int32_t *tri_deg,
+                       double alpha);
+
+/* Graph sizes and p_ext of the resident graph (src/graph.hpp:25-27). */
+int scd_graph_info(scd_ctx *ctx, uint32_t *n, uint32_t *m, double *clustering_coef);
+
+/* Copies the resident graph out in the binary-format layout; any pointer may
+ * be NULL (what `convert` writes, src/convert.cpp:430-455). */
+int scd_graph_download(scd_ctx *ctx, uint32_t *indices, uint32_t *adj, int32_t *tri,
+                       int32_t *tri_deg);
+
+/* create_initial_partition (src/scd.cpp:113-171) on the device, including its
+ * collect_stats; leaves the labels as both current and best labels. */
+int scd_initial_partition(scd_ctx *ctx, uint32_t *num_communities);
+
+/* Replaces cuda_labels_to_device(labels) (src/cuda.hpp:25, src/cuda.cu:150-174):
+ * sets current and best labels (n entries) and collects community statistics. */
+int scd_labels_to_device(scd_ctx *ctx, const uint32_t *labels);
+
+/* compute_wcc (src/wcc.cpp:31-141) of the current labels. */
+int scd_compute_wcc(scd_ctx *ctx, double *wcc);
+
+/* Replaces cuda_improve_labels(&wcc) (src/cuda.hpp:26, src/cuda.cu:176-361):
+ * one refinement iteration — improve_partition (src/scd.cpp:221-341),
+ * collect_stats (src/scd.cpp:57-111), compute_wcc — returning the new WCC. */
+int scd_improve_labels(scd_ctx *ctx, double *wcc);
+
+/* Replaces cuda_store_labels() (src/cuda.hpp:27): best labels := current labels. */
+int scd_store_labels(scd_ctx *ctx);
+
+/* Replaces cuda_labels_from_device(labels) (src/cuda.hpp:28): copies the best labels out. */
+int scd_labels_from_device(scd_ctx *ctx, uint32_t *labels);
+
+/* Current (not best) labels and the community statistics of the current
+ * labels (sizes, ext_edges, int_edges of src/scd.hpp:25-31); any pointer may be
+ * NULL; arrays hold *num_communities entries. */
+int scd_current_labels(scd_ctx *ctx, uint32_t *labels);
+int scd_community_stats(scd_ctx *ctx, int32_t *sizes, int32_t *ext_edges, int32_t *int_edges,
+                        uint32_t *num_communities);
+
+typedef struct {
+    int32_t iterations;            /* src/main-gpu.cpp:72-75 iters              */
+    double initial_wcc;            /* src/main-gpu.cpp:55                       */
+    double best_wcc;               /* the "WCC:" of the final block             */
+    uint32_t initial_communities;  /* communities of the initial partition      */
+    uint32_t printed_communities;  /* "num. communities:" as the reference prints
+                                      it (src/scd.cpp:32-55, inverted branch)    */
+    uint32_t distinct_communities; /* true number of distinct valid best labels */
+    double ms_partition;           /* initial partition + initial WCC           */
+    double ms_iterations;          /* refinement loop                           */
+} scd_result;
+
+/* The whole refinement loop of src/main-gpu.cpp:54-110 after the graph is
+ * resident: initial partition (unless labels were already set), initial WCC,
+ * iterations until wcc < best*(1+threshold) or max_iters, best-label
+ * tracking.  wcc_trace (nullable) receives up to max_iters per-iteration WCCs.
+ * Returns SCD_ERR_LIMIT if max_iters was reached without convergence (the
+ * reference loops forever when the WCC stays 0, src/main.cpp:77). */
+int scd_run(scd_ctx *ctx, double threshold, int max_iters, double *wcc_trace, scd_result *res);
+
+/* Device memory currently held by the context (bytes). */
+int scd_memory_usage(scd_ctx *ctx, uint64_t *bytes);
+
+/* Number of kernels this context launched so far (for launch accounting). */
+int scd_kernel_launches(scd_ctx *ctx, uint64_t *count);
+
+/* The CUDA stream (cudaStream_t) all work of the context is ordered on. */
+int scd_stream(scd_ctx *ctx, void **stream);
+
+/* Phase timers (CUDA events on the context's stream, recorded only when the
+ * context was created with SCD_FLAG_PROFILE): accumulated milliseconds and
+ * number of timed launches of a phase.  Phases: "convert", "tc" (triangle
+ * counting kernel of the preprocessing), "partition", "improve", "stats",
+ * "wcc_tc" (internal-triangle kernel), "wcc".  scd_profile_reset clears them. */
+int scd_profile_get(scd_ctx *ctx, const char *phase, double *total_ms, uint64_t *count);
+int scd_profile_reset(scd_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,170 @@
+"""GPU engine vs the reference (golden fixtures) and vs the oracle, through the C ABI.
+
+Bar (from the task): the converted graph (CSR, tri, tri_deg) and the initial
+partition bit-exact; per-iteration labels identical under the reference's
+tie-breaking rule; WCC within 1e-6 relative (the engine sums per-vertex terms
+in a fixed tree order, the reference in index order, so the last bits of the
+sum may differ).  p_ext is summed in the reference's single-thread order and
+must be bit-exact.
+"""
+import numpy as np
+import pytest
+
+import golden_data as G
+import oracle as O
+import scd_gb300 as S
+import scdgen
+
+pytestmark = pytest.mark.gpu
+WCC_RTOL = 1e-6
+CASES = G.cases()
+TRACED = [c for c in CASES if G.manifest()[c].get("iters")]
+
+
+@pytest.fixture(scope="module")
+def engine():
+    e = S.Engine(0)
+    yield e
+    e.close()
+
+
+def rel(a, b):
+    return abs(a - b) / max(abs(b), 1e-300)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_convert_bit_exact_with_reference(engine, name):
+    engine.convert_edges(G.pairs(name))
+    assert engine.graph_bytes() == G.graph_bytes(name)
+
+
+def _divergence_report(g, p_ext, labels, stats, got, want):
+    bad = np.nonzero(got != want)[0]
+    return f"{len(bad)} vertices differ, first {bad[:10].tolist()}: got {got[bad[:10]].tolist()} want {want[bad[:10]].tolist()}"
+
+
+@pytest.mark.parametrize("name", TRACED)
+def test_iterations_match_reference_trace(engine, name):
+    g = O.Graph.from_bytes(G.graph_bytes(name))
+    tr = G.trace(name)
+    engine.transfer_graph(g)
+    n, m, cc = engine.graph_info()
+    assert (n, m) == (tr["n"], tr["m"])
+    assert cc == tr["p_ext"], "p_ext must be the reference's single-thread sum"
+    nc = engine.initial_partition()
+    assert nc == tr["num_comms"]
+    assert np.array_equal(engine.current_labels(), tr["initial_labels"])
+    assert np.array_equal(np.stack(engine.community_stats()), tr["initial_stats"])
+    w0 = engine.compute_wcc()
+    assert rel(w0, tr["initial_wcc"]) < WCC_RTOL
+    for i in range(tr["iters"]):
+        w = engine.improve_labels()
+        got = engine.current_labels()
+        assert np.array_equal(got, tr["labels"][i]), f"iteration {i}: " + _divergence_report(
+            g, cc, None, None, got, tr["labels"][i])
+        assert np.array_equal(np.stack(engine.community_stats()), tr["stats"][i])
+        assert rel(w, tr["wcc"][i]) < WCC_RTOL
+
+
+@pytest.mark.parametrize("name", TRACED)
+def test_run_loop_matches_reference(engine, name):
+    g = O.Graph.from_bytes(G.graph_bytes(name))
+    tr = G.trace(name)
+    engine.transfer_graph(g)
+    r = engine.run(0.01, 1000)
+    assert r["iterations"] == tr["iters"]
+    assert r["initial_communities"] == tr["num_comms"]
+    assert rel(r["best_wcc"], tr["best_wcc"]) < WCC_RTOL
+    assert np.array_equal(engine.labels_from_device(), tr["best_labels"])
+    assert r["printed_communities"] == tr["printed_comms"]
+    for a, b in zip(r["wcc"], tr["wcc"]):
+        assert rel(a, b) < WCC_RTOL
+
+
+RANDOM_GRAPHS = [
+    ("planted", lambda s: scdgen.planted(3000 + 500 * s, 10.0 + 2 * s, 0.05 + 0.07 * s, 20, 100, seed=100 + s)),
+    ("rmat", lambda s: scdgen.rmat(10 + s % 4, 8 + 4 * (s % 3), seed=200 + s)),
+    ("chunglu", lambda s: scdgen.chunglu(4000 + 1000 * s, 2.1, 5.0, 300.0 + 200 * s, 0.2, 10, 200, seed=300 + s)),
+]
+
+
+@pytest.mark.parametrize("kind,make", RANDOM_GRAPHS, ids=[k for k, _ in RANDOM_GRAPHS])
+@pytest.mark.parametrize("seed", range(4))
+def test_random_graphs_against_oracle(engine, kind, make, seed):
+    pairs = make(seed)
+    # shuffle the record order and flip some pairs: exercises first-appearance renumbering
+    rng = np.random.default_rng(seed)
+    pairs = pairs[rng.permutation(pairs.shape[0])]
+    dup = pairs[rng.integers(0, pairs.shape[0], pairs.shape[0] // 20)]
+    pairs = np.concatenate([pairs, dup, np.array([[7, 7], [3, 3]], np.uint32)])
+    ref, _ = O.convert(pairs)
+    engine.convert_edges(pairs)
+    assert engine.graph_bytes() == ref.to_bytes()
+    if ref.n == 0:
+        return
+    r = O.run(ref, max_iters=200)
+    n, m, cc = engine.graph_info()
+    assert cc == O.clustering_coef(ref)
+    engine.initial_partition()
+    assert np.array_equal(engine.current_labels(), r["initial_labels"])
+    for i in range(len(r["wcc"])):
+        w = engine.improve_labels()
+        assert np.array_equal(engine.current_labels(), r["labels"][i]), f"iteration {i}"
+        assert rel(w, r["wcc"][i]) < WCC_RTOL
+
+
+def test_empty_and_degenerate_inputs(engine):
+    engine.convert_edges(np.zeros((0, 2), np.uint32))
+    assert engine.graph_info()[:2] == (0, 0)
+    assert engine.graph_bytes() == O.convert(np.zeros((0, 2), np.uint32))[0].to_bytes()
+    loops = np.array([[5, 5], [9, 9]], np.uint32)
+    engine.convert_edges(loops)
+    assert engine.graph_bytes() == O.convert(loops)[0].to_bytes()
+    tri = np.array([[0, 1], [1, 2], [0, 2]], np.uint32)
+    engine.convert_edges(tri)
+    assert engine.graph_bytes() == O.convert(tri)[0].to_bytes()
+    r = engine.run()
+    assert r["iterations"] >= 1
+
+
+def test_call_order_and_argument_errors(engine):
+    e = S.Engine(0)
+    with pytest.raises(S.ScdError) as ex:
+        e.improve_labels()
+    assert ex.value.status == -4
+    e.convert_edges(G.pairs("planted_2k_mu03"))
+    with pytest.raises(S.ScdError) as ex:
+        e.compute_wcc()
+    assert ex.value.status == -4
+    n = e.graph_info()[0]
+    with pytest.raises(S.ScdError) as ex:
+        e.labels_to_device(np.full(n, n + 5, np.uint32))
+    assert ex.value.status == -1
+    e.close()
+
+
+def test_labels_to_device_roundtrip(engine):
+    name = "planted_2k_mu03"
+    g = O.Graph.from_bytes(G.graph_bytes(name))
+    tr = G.trace(name)
+    engine.transfer_graph(g)
+    engine.labels_to_device(tr["labels"][2])
+    st = np.stack(engine.community_stats())
+    k = st.shape[1]
+    assert np.array_equal(st, tr["stats"][2][:, :k]) and not tr["stats"][2][:, k:].any()
+    engine.improve_labels()
+    assert np.array_equal(engine.current_labels(), tr["labels"][3])
+
+
+def test_rmat16_full_pipeline_against_oracle(engine):
+    pairs = scdgen.rmat(16, 16, seed=22)
+    ref, _ = O.convert(pairs)
+    engine.convert_edges(pairs)
+    assert engine.graph_bytes() == ref.to_bytes()
+    r = O.run(ref, max_iters=50)
+    engine.initial_partition()
+    assert np.array_equal(engine.current_labels(), r["initial_labels"])
+    for i in range(len(r["wcc"])):
+        w = engine.improve_labels()
+        assert np.array_equal(engine.current_labels(), r["labels"][i])
+        assert rel(w, r["wcc"][i]) < WCC_RTOL
