@@ -70,6 +70,7 @@ def lib():
             "scd_stream": ([P, ctypes.POINTER(P)], i32),
             "scd_profile_get": ([P, ctypes.c_char_p, ctypes.POINTER(dbl), ctypes.POINTER(u64)], i32),
             "scd_profile_reset": ([P], i32),
+            "scd_wcc_static": ([P, P, P, P, P, P, u32, dbl, P, P], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)

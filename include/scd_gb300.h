@@ -142,6 +142,31 @@ int scd_stream(scd_ctx *ctx, void **stream);
 int scd_profile_get(scd_ctx *ctx, const char *phase, double *total_ms, uint64_t *count);
 int scd_profile_reset(scd_ctx *ctx);
 
+/* WCC of a labelling without any device allocation.  It has no counterpart in
+ * the reference: it exists for callers that cannot let a library call
+ * cudaMalloc/cudaFree — a serving process whose memory pool already holds the
+ * free device memory, a plugin host that accounts for every allocation itself,
+ * or a latency-critical loop that cannot take the device-wide synchronisation
+ * of cudaFree.  The caller passes device pointers to the graph in the
+ * binary-format layout (indices[n+1], adj, tri[n], tri_deg[n]), the labels[n]
+ * and the size of every community its labels use (sizes[label]), and a device
+ * pointer wcc that receives one double; work is queued on stream (a
+ * cudaStream_t, NULL for the default stream) of the current device and the
+ * call returns without waiting.  The value equals scd_compute_wcc's for the
+ * same graph and labels.
+ * Scratch: a fixed array of SCD_WCC_STATIC_MAX_VERTICES/2048 doubles (64 KB)
+ * inside the library, allocated when the library is loaded and held by every
+ * GPU that uses it until the process exits; n above SCD_WCC_STATIC_MAX_VERTICES
+ * returns SCD_ERR_LIMIT.  All calls share that array: calls that may overlap
+ * on the GPU (different streams without ordering) race and must be ordered by
+ * the caller.  The first call on a device looks up the array's device address
+ * and should come before any stream capture.
+ * Returns SCD_OK, SCD_ERR_ARG (NULL pointer), SCD_ERR_LIMIT or SCD_ERR_CUDA. */
+#define SCD_WCC_STATIC_MAX_VERTICES (1u << 24)
+int scd_wcc_static(const uint32_t *indices, const uint32_t *adj, const int32_t *tri,
+                   const int32_t *tri_deg, const uint32_t *labels, const int32_t *sizes, uint32_t n,
+                   double alpha, double *wcc, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,70 @@
+"""scd_wcc_static: WCC without any device allocation by the library.
+
+Some callers cannot let a library allocate device memory: a serving process
+whose pool already holds the free HBM, a plugin host that accounts for every
+allocation itself, or a loop that cannot take cudaFree's device-wide
+synchronisation.  They own every buffer and call scd_wcc_static with device
+pointers; its only scratch is a fixed array inside the library.
+
+This file is collected last on purpose (other GPU tests run first in a run that
+stops at the first failure).  It must pass alone in a fresh process and after
+the other tests, so it builds all of its own state.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import golden_data as G
+import scd_gb300 as S
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-6   # the WCC tolerance of the parity tests
+
+
+def _device(t, torch):
+    return torch.from_numpy(np.ascontiguousarray(t)).cuda()
+
+
+def _static_wcc(lib, torch, graph, labels, sizes, alpha=1.0):
+    """Calls scd_wcc_static through the C ABI with caller-owned device buffers."""
+    ind = _device(graph["indices"].view(np.int32), torch)
+    adj = _device(graph["adj"].view(np.int32) if graph["adj"].size else np.zeros(1, np.int32), torch)
+    tri = _device(graph["tri"], torch)
+    tdg = _device(graph["tri_deg"], torch)
+    lab = _device(labels.view(np.int32), torch)
+    siz = _device(sizes if sizes.size else np.zeros(1, np.int32), torch)
+    out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.scd_wcc_static(ind.data_ptr(), adj.data_ptr(), tri.data_ptr(), tdg.data_ptr(), lab.data_ptr(),
+                            siz.data_ptr(), graph["n"], alpha, out.data_ptr(), stream)
+    assert rc == S.OK, rc
+    torch.cuda.synchronize()
+    return float(out.item())
+
+
+def test_static_wcc_matches_engine_on_two_calls_in_a_row():
+    torch = pytest.importorskip("torch")
+    lib = S.lib()
+    with S.Engine(0) as eng:
+        eng.convert_edges(G.pairs("planted_10k"))
+        graph = eng.graph_download()
+        eng.initial_partition()
+        want = [eng.compute_wcc()]
+        labels = [eng.current_labels()]
+        sizes = [eng.community_stats()[0].copy()]
+        want.append(eng.improve_labels())
+        labels.append(eng.current_labels())
+        sizes.append(eng.community_stats()[0].copy())
+    got = [_static_wcc(lib, torch, graph, labels[k], sizes[k]) for k in range(2)]
+    for g, w in zip(got, want):
+        assert abs(g - w) <= RTOL * abs(w), (g, w)
+    assert got[0] != got[1]   # the second call saw the second labelling
+
+
+def test_static_wcc_limits_and_arguments():
+    lib = S.lib()
+    dummy = ctypes.c_void_p(1)
+    over = S.lib().scd_wcc_static(dummy, dummy, dummy, dummy, dummy, dummy, (1 << 24) + 1, 1.0, dummy, None)
+    assert over == -7   # SCD_ERR_LIMIT, rejected before any GPU work
+    assert lib.scd_wcc_static(None, None, None, None, None, None, 10, 1.0, None, None) == -1
