@@ -10,8 +10,6 @@ namespace scd {
 namespace {
 
 constexpr unsigned TPB = 256;
-constexpr uint32_t SMALL_MAX = 32;     // warp kernel: one lane per neighbour
-constexpr uint32_t MID_MAX = 4096;     // CTA kernel, shared-memory table of <= 8192 entries
 
 // neighbours with a smaller id: the out-list of the degree orientation
 __global__ void k_nlow(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
@@ -162,6 +160,8 @@ void Ctx::free_all() {
     itri = itdeg = nullptr;
     wcc_part = wcc_sum = nullptr;
     big_tables = nullptr;
+    pin64 = nullptr;
+    pin32 = nullptr;
     num_comms = 0;
 }
 
@@ -175,13 +175,16 @@ void finish_graph(Ctx &c) {
         k_nlow<<<grid_for(n, TPB), TPB, 0, s>>>(n, g.indices, g.adj, g.nlow);
         CK_LAUNCH("k_nlow");
     }
-    g.n_small = class_list(c, 0, SMALL_MAX, &g.cls_small);
-    g.n_mid = class_list(c, SMALL_MAX, MID_MAX, &g.cls_mid);
-    g.n_big = class_list(c, MID_MAX, 0xffffffffu, &g.cls_big);
-    g.big_table_off = c.alloc<uint64_t>((size_t)g.n_big + 1);
-    if (g.n_big) {
-        scan_exclusive<uint64_t>(TableWords{g.cls_big, g.indices}, g.big_table_off, g.n_big, s);
-        CK(cudaMemcpyAsync(&g.big_table_words, g.big_table_off + g.n_big, 8, cudaMemcpyDeviceToHost, s));
+    uint32_t lo = 0;
+    for (int k = 0; k < DegreeClasses::K; k++) {
+        g.cls.count[k] = class_list(c, lo, DegreeClasses::upper[k], &g.cls.list[k]);
+        lo = DegreeClasses::upper[k];
+    }
+    const uint32_t n_big = g.cls.count[DegreeClasses::K - 1];
+    g.big_table_off = c.alloc<uint64_t>((size_t)n_big + 1);
+    if (n_big) {
+        scan_exclusive<uint64_t>(TableWords{g.cls.list[DegreeClasses::K - 1], g.indices}, g.big_table_off, n_big, s);
+        CK(cudaMemcpyAsync(&g.big_table_words, g.big_table_off + n_big, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         c.big_tables = c.alloc<uint32_t>(g.big_table_words);
     }
@@ -193,6 +196,8 @@ void finish_graph(Ctx &c) {
         c.st[k].ext = c.alloc<int32_t>(n);
         c.st[k].intl = c.alloc<int32_t>(n);
     }
+    c.pin64 = c.alloc<double>(n);
+    c.pin32 = c.alloc<float2>(n);
     c.slot_cnt = c.alloc<uint32_t>(2 * (size_t)g.m);
     c.itri = c.alloc<int32_t>(n);
     c.itdeg = c.alloc<int32_t>(n);

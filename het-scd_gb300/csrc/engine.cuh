@@ -21,6 +21,14 @@
 
 namespace scd {
 
+// vertex lists by degree: (0,8], (8,16], (16,32], (32,256], (256,4096], > 4096
+struct DegreeClasses {
+    static constexpr int K = 6;
+    static constexpr uint32_t upper[K] = {8, 16, 32, 256, 4096, 0xffffffffu};
+    uint32_t *list[K] = {};
+    uint32_t count[K] = {};
+};
+
 struct Graph {
     uint32_t n = 0, m = 0;
     uint32_t *indices = nullptr, *adj = nullptr, *nlow = nullptr;
@@ -28,10 +36,9 @@ struct Graph {
     double p_ext = 0.0;
     double *p_ext_dev = nullptr;
     uint32_t max_deg = 0;
-    // degree classes for the improve kernels (vertex lists), built once per graph
-    uint32_t *cls_small = nullptr, *cls_mid = nullptr, *cls_big = nullptr;
-    uint32_t n_small = 0, n_mid = 0, n_big = 0;
-    uint64_t *big_table_off = nullptr;   // hash-table offsets of the big class
+    // degree buckets of the improve kernels, built once per graph
+    DegreeClasses cls;
+    uint64_t *big_table_off = nullptr;   // hash-table offsets of the last bucket
     uint64_t big_table_words = 0;
 };
 
@@ -88,7 +95,9 @@ struct Ctx {
     uint32_t *slot_cnt = nullptr;
     int32_t *itri = nullptr, *itdeg = nullptr;
     double *wcc_part = nullptr, *wcc_sum = nullptr, *wcc_host = nullptr;
-    uint32_t *big_tables = nullptr;   // global hash tables of the big class
+    uint32_t *big_tables = nullptr;   // global hash tables of the last degree bucket
+    double *pin64 = nullptr;          // per-community p_in of the current statistics
+    float2 *pin32 = nullptr;          // and its FP32 enclosure
     uint32_t *work_counter = nullptr; // dynamic work distribution
 
     PhaseTimers timers;

@@ -1,0 +1,331 @@
+// improve_partition (src/scd.cpp:221-341) on the device.
+//
+// For every vertex p the multiset of its neighbours' labels (old labels) is
+// reduced to (label, frequency) pairs without sorting:
+//   degree <= 32     a group of 8, 16 or 32 lanes of a warp, one lane per
+//                    neighbour; __match_any_sync finds equal labels (groups
+//                    are separated by a lane mask), the lowest lane of each
+//                    equal-label set owns the label;
+//   33 .. 4096       one CTA per vertex, open-addressing hash table of
+//                    (label, count) in shared memory;
+//   > 4096           one CTA per vertex, per-vertex hash table in global memory.
+// Each distinct label other than p's own first gets an FP32 interval
+// enclosure of its FP64 gain (gain_interval.cuh).  The own label's gain (the
+// remove gain) is always evaluated exactly; a foreign label is evaluated
+// exactly only if its interval could still hold the maximum (upper bound >= the
+// best lower bound and > 0, or undecidable).  The winner is the largest exact
+// positive gain, ties to the smaller label — the candidate the reference's
+// ascending scan with a strict '>' keeps (src/scd.cpp:313-316) — and the
+// decision of src/scd.cpp:321-330 follows.  Labels update Jacobi-style.
+#include "engine.cuh"
+#include "gain_interval.cuh"
+
+namespace scd {
+
+namespace {
+
+constexpr unsigned TPB = 256;
+
+struct ImproveArgs {
+    const uint32_t *indices, *adj, *labels;
+    Stats st;
+    const double *pin64;   // p_in of every community (src/scd.cpp:296-298)
+    const float2 *pin32;   // its FP32 enclosure
+    const double *p_ext_ptr;
+    double alpha;
+    uint32_t *next;
+};
+
+__device__ __forceinline__ bool better(double g1, uint32_t l1, double g2, uint32_t l2) {
+    return g1 > g2 || (g1 == g2 && l1 < l2);
+}
+
+// exact FP64 gain of moving p (degree deg, label mine) to label l seen freq times
+__device__ __forceinline__ double exact_gain(const ImproveArgs &a, uint32_t l, uint32_t freq, uint32_t deg,
+                                             uint32_t mine, double p_ext) {
+    int size = a.st.sizes[l], ext = a.st.ext[l];
+    double p_in;
+    if (l == mine) {
+        int in = a.st.intl[l] / 2;
+        size--;
+        ext += (int)(freq - (deg - freq));
+        in -= (int)freq;
+        p_in = community_p_in(size, in);
+    } else {
+        p_in = a.pin64[l];
+    }
+    return wcc_gain(size, (int)freq, (int)deg - (int)freq, ext, p_in, p_ext, a.alpha);
+}
+
+__device__ __forceinline__ Iv interval_gain(const ImproveArgs &a, uint32_t l, uint32_t freq, uint32_t deg,
+                                            Iv p_ext, Iv alpha, bool *exact_needed) {
+    const float2 pin = a.pin32[l];
+    return wcc_gain_iv(a.st.sizes[l], (int)freq, (int)deg - (int)freq, a.st.ext[l], Iv{pin.x, pin.y}, p_ext, alpha,
+                       exact_needed);
+}
+
+__device__ __forceinline__ uint32_t decide(double best_gain, uint32_t best_label, double remove_gain,
+                                           uint32_t mine) {
+    const double insert = dadd(best_gain, remove_gain);
+    if (insert > remove_gain && insert > 0.0) return best_label;
+    if (remove_gain > 0) return INVALID;
+    return mine;
+}
+
+__global__ void k_comm_prep(uint32_t nc, Stats st, double *pin64, float2 *pin32) {
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < nc; l += gridDim.x * blockDim.x) {
+        const double p = community_p_in(st.sizes[l], st.intl[l] / 2);
+        pin64[l] = p;
+        pin32[l] = make_float2(__double2float_rd(p), __double2float_ru(p));
+    }
+}
+
+// ---- degree <= G: groups of G lanes ---------------------------------------
+
+template <int G>
+__global__ void __launch_bounds__(TPB)
+k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
+    constexpr int PER_WARP = 32 / G;
+    const int lane = threadIdx.x & 31, gl = lane % G, g0 = lane - gl;
+    const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << g0);
+    const double p_ext = *a.p_ext_ptr;
+    const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * PER_WARP < count; w += warps) {
+        const uint32_t slot = w * PER_WARP + lane / G;
+        const bool active = slot < count;
+        const uint32_t p = active ? verts[slot] : 0;
+        const uint32_t beg = active ? a.indices[p] : 0;
+        const uint32_t deg = active ? a.indices[p + 1] - beg : 0;
+        const uint32_t mine = active ? a.labels[p] : INVALID;
+        const uint32_t l = (uint32_t)gl < deg ? a.labels[a.adj[beg + gl]] : INVALID;
+        const unsigned peers = __match_any_sync(FULL, l) & gmask;
+        const bool owner = l != INVALID && lane == __ffs(peers) - 1;
+        const uint32_t freq = __popc(peers);
+        // own label: exact remove gain
+        const bool own = owner && l == mine;
+        const double g_own = own ? exact_gain(a, l, freq, deg, mine, p_ext) : 0.0;
+        const unsigned own_lanes = __ballot_sync(FULL, own) & gmask;
+        const double own_val = __shfl_sync(FULL, g_own, own_lanes ? __ffs(own_lanes) - 1 : lane);
+        const double remove_gain = own_lanes ? -own_val : 0.0;
+        // foreign labels: interval first
+        const bool cand = owner && l != mine;
+        bool need = false;
+        Iv iv = {0.f, 0.f};
+        if (cand) iv = interval_gain(a, l, freq, deg, pe, al, &need);
+        float m = (cand && !need) ? iv.lo : -INFINITY;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+        const bool survive = cand && (need || (iv.hi > 0.f && iv.hi >= m));
+        double bg = 0.0;
+        uint32_t bl = INVALID;
+        if (survive) {
+            const double gx = exact_gain(a, l, freq, deg, mine, p_ext);
+            if (gx > 0.0) {
+                bg = gx;
+                bl = l;
+            }
+        }
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            const double og = __shfl_xor_sync(FULL, bg, o);
+            const uint32_t ol = __shfl_xor_sync(FULL, bl, o);
+            if (ol != INVALID && (bl == INVALID || better(og, ol, bg, bl))) {
+                bg = og;
+                bl = ol;
+            }
+        }
+        if (active && gl == 0) a.next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, remove_gain, mine);
+    }
+}
+
+// ---- degree > 32: one CTA per vertex, (label, count) hash table -------------
+
+__device__ __forceinline__ uint32_t hash32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+template <int THREADS>
+__device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, uint32_t *vals, uint32_t cap,
+                            double p_ext, Iv pe, Iv al) {
+    __shared__ double s_gain[THREADS / 32];
+    __shared__ uint32_t s_label[THREADS / 32];
+    __shared__ float s_lo[THREADS / 32];
+    __shared__ double s_remove;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t beg = a.indices[p], deg = a.indices[p + 1] - beg, mine = a.labels[p];
+    const uint32_t mask = cap - 1;
+    for (uint32_t i = threadIdx.x; i < cap; i += THREADS) {
+        keys[i] = INVALID;
+        vals[i] = 0;
+    }
+    if (threadIdx.x == 0) s_remove = 0.0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < deg; i += THREADS) {
+        const uint32_t l = a.labels[a.adj[beg + i]];
+        if (l == INVALID) continue;
+        uint32_t h = hash32(l) & mask;
+        while (true) {
+            uint32_t k = keys[h];
+            if (k == INVALID) {
+                k = atomicCAS(keys + h, INVALID, l);
+                if (k == INVALID) k = l;
+            }
+            if (k == l) {
+                atomicAdd(vals + h, 1u);
+                break;
+            }
+            h = (h + 1) & mask;
+        }
+    }
+    __syncthreads();
+    // pass 1: own gain (exact) and the best lower bound among foreign labels
+    float m = -INFINITY;
+    for (uint32_t i = threadIdx.x; i < cap; i += THREADS) {
+        const uint32_t l = keys[i];
+        if (l == INVALID) continue;
+        if (l == mine) {
+            s_remove = -exact_gain(a, l, vals[i], deg, mine, p_ext);
+        } else {
+            bool need = false;
+            const Iv iv = interval_gain(a, l, vals[i], deg, pe, al, &need);
+            if (!need) m = fmaxf(m, iv.lo);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+    if (lane == 0) s_lo[warp] = m;
+    __syncthreads();
+    m = s_lo[0];
+#pragma unroll
+    for (int w = 1; w < THREADS / 32; w++) m = fmaxf(m, s_lo[w]);
+    // pass 2: exact gains of the surviving labels
+    double bg = 0.0;
+    uint32_t bl = INVALID;
+    for (uint32_t i = threadIdx.x; i < cap; i += THREADS) {
+        const uint32_t l = keys[i];
+        if (l == INVALID || l == mine) continue;
+        bool need = false;
+        const Iv iv = interval_gain(a, l, vals[i], deg, pe, al, &need);
+        if (need || (iv.hi > 0.f && iv.hi >= m)) {
+            const double g = exact_gain(a, l, vals[i], deg, mine, p_ext);
+            if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
+                bg = g;
+                bl = l;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double og = __shfl_xor_sync(FULL, bg, o);
+        const uint32_t ol = __shfl_xor_sync(FULL, bl, o);
+        if (ol != INVALID && (bl == INVALID || better(og, ol, bg, bl))) {
+            bg = og;
+            bl = ol;
+        }
+    }
+    if (lane == 0) {
+        s_gain[warp] = bg;
+        s_label[warp] = bl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < THREADS / 32; w++)
+            if (s_label[w] != INVALID && (bl == INVALID || better(s_gain[w], s_label[w], bg, bl))) {
+                bg = s_gain[w];
+                bl = s_label[w];
+            }
+        a.next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, s_remove, mine);
+    }
+    __syncthreads();
+}
+
+template <int THREADS, uint32_t CAP>
+__global__ void __launch_bounds__(THREADS)
+k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
+    extern __shared__ uint32_t smem[];
+    uint32_t *keys = smem, *vals = smem + CAP;
+    const double p_ext = *a.p_ext_ptr;
+    const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
+    for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const uint32_t p = verts[i];
+        const uint32_t deg = a.indices[p + 1] - a.indices[p];
+        uint32_t cap = 64;
+        while (cap < 2 * deg) cap <<= 1;
+        improve_cta<THREADS>(a, p, keys, vals, cap, p_ext, pe, al);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_improve_global(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a, uint32_t *tables,
+                 const uint64_t *__restrict__ table_off) {
+    const double p_ext = *a.p_ext_ptr;
+    const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
+    for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const uint64_t off = table_off[i];
+        const uint32_t cap = (uint32_t)((table_off[i + 1] - off) / 2);
+        improve_cta<256>(a, verts[i], tables + off, tables + off + cap, cap, p_ext, pe, al);
+    }
+}
+
+template <int THREADS, uint32_t CAP>
+void launch_cta(const uint32_t *verts, uint32_t count, const ImproveArgs &a, cudaStream_t s, unsigned max_grid) {
+    const size_t smem = 2 * CAP * sizeof(uint32_t);
+    if (smem > 48 * 1024)
+        CK(cudaFuncSetAttribute((const void *)k_improve_cta<THREADS, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem));
+    k_improve_cta<THREADS, CAP><<<grid_for(count, 1, max_grid), THREADS, smem, s>>>(verts, count, a);
+    CK_LAUNCH("k_improve_cta");
+}
+
+}  // namespace
+
+void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next) {
+    const Graph &g = c.g;
+    cudaStream_t s = c.stream;
+    if (g.n == 0) return;
+    PhaseScope ph(c, "improve");
+    if (c.num_comms) {
+        k_comm_prep<<<grid_for(c.num_comms, TPB), TPB, 0, s>>>(c.num_comms, st, c.pin64, c.pin32);
+        CK_LAUNCH("k_comm_prep");
+        c.launches++;
+    }
+    ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.pin32, g.p_ext_dev, c.alpha, next};
+    const DegreeClasses &k = g.cls;
+    if (k.count[0]) {
+        k_improve_group<8><<<grid_for((uint64_t)k.count[0] * 8, TPB), TPB, 0, s>>>(k.list[0], k.count[0], a);
+        CK_LAUNCH("k_improve_group8");
+        c.launches++;
+    }
+    if (k.count[1]) {
+        k_improve_group<16><<<grid_for((uint64_t)k.count[1] * 16, TPB), TPB, 0, s>>>(k.list[1], k.count[1], a);
+        CK_LAUNCH("k_improve_group16");
+        c.launches++;
+    }
+    if (k.count[2]) {
+        k_improve_group<32><<<grid_for((uint64_t)k.count[2] * 32, TPB), TPB, 0, s>>>(k.list[2], k.count[2], a);
+        CK_LAUNCH("k_improve_group32");
+        c.launches++;
+    }
+    if (k.count[3]) {
+        launch_cta<128, 512>(k.list[3], k.count[3], a, s, 152 * 16);
+        c.launches++;
+    }
+    if (k.count[4]) {
+        launch_cta<256, 8192>(k.list[4], k.count[4], a, s, 152 * 3);
+        c.launches++;
+    }
+    if (k.count[5]) {
+        k_improve_global<<<grid_for(k.count[5], 1, 152 * 2), 256, 0, s>>>(k.list[5], k.count[5], a, c.big_tables,
+                                                                         g.big_table_off);
+        CK_LAUNCH("k_improve_global");
+        c.launches++;
+    }
+}
+
+}  // namespace scd

@@ -1,17 +1,6 @@
-// One refinement iteration on the device: improve_partition
-// (src/scd.cpp:221-341), collect_stats (src/scd.cpp:57-111) and compute_wcc
-// (src/wcc.cpp:31-141), plus the clustering coefficient p_ext
-// (src/graph.cpp:57-68).
-//
-// improve: for every vertex, the multiset of its neighbours' labels is reduced
-// to (label, frequency) runs without sorting: degree <= 32 by one warp with
-// __match_any_sync (one lane per neighbour); larger degrees by one CTA with an
-// open-addressing hash table in shared memory (global memory for the few
-// vertices whose table does not fit).  Each distinct label's FP64 gain is
-// evaluated once; the winner is the maximal positive gain, ties to the
-// smallest label, which is what the reference's ascending scan with a strict
-// '>' picks (src/scd.cpp:313-316).  Labels are updated Jacobi-style
-// (old labels in, new labels out).
+// Community statistics (collect_stats, src/scd.cpp:57-111), the WCC metric
+// (compute_wcc, src/wcc.cpp:31-141) and the clustering coefficient p_ext
+// (src/graph.cpp:57-68); the label improvement itself is in improve.cu.
 //
 // wcc: internal triangles per edge by the oriented counting kernel restricted
 // to same-label triangles, per-vertex sums, per-vertex WCC terms and a
@@ -24,200 +13,6 @@ namespace scd {
 namespace {
 
 constexpr unsigned TPB = 256;
-
-struct Best {
-    double gain;
-    uint32_t label;
-};
-
-// (g1,l1) better than (g2,l2): larger gain, ties to the smaller label
-__device__ __forceinline__ bool better(double g1, uint32_t l1, double g2, uint32_t l2) {
-    return g1 > g2 || (g1 == g2 && l1 < l2);
-}
-
-__device__ __forceinline__ double gain_of(uint32_t l, uint32_t freq, uint32_t deg, uint32_t mine,
-                                          const Stats &st, double p_ext, double alpha) {
-    int size = st.sizes[l], ext = st.ext[l], in = st.intl[l] / 2;
-    if (l == mine) {
-        size--;
-        ext += (int)(freq - (deg - freq));
-        in -= (int)freq;
-    }
-    const double p_in = community_p_in(size, in);
-    return wcc_gain(size, (int)freq, (int)deg - (int)freq, ext, p_in, p_ext, alpha);
-}
-
-// decision of src/scd.cpp:321-330
-__device__ __forceinline__ uint32_t decide(double best_gain, uint32_t best_label, double remove_gain,
-                                           uint32_t mine) {
-    const double insert = dadd(best_gain, remove_gain);
-    if (insert > remove_gain && insert > 0.0) return best_label;
-    if (remove_gain > 0) return INVALID;
-    return mine;
-}
-
-// ---- degree <= 32: one warp per vertex -----------------------------------
-
-__global__ void __launch_bounds__(TPB)
-k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, const uint32_t *__restrict__ indices,
-               const uint32_t *__restrict__ adj, const uint32_t *__restrict__ labels, Stats st,
-               const double *__restrict__ p_ext_ptr, double alpha, uint32_t *next) {
-    const int lane = threadIdx.x & 31;
-    const double p_ext = *p_ext_ptr;
-    for (uint32_t wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < count;
-         wi += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t p = verts[wi];
-        const uint32_t beg = indices[p], deg = indices[p + 1] - beg;
-        const uint32_t mine = labels[p];
-        const uint32_t l = lane < (int)deg ? labels[adj[beg + lane]] : INVALID;
-        const unsigned peers = __match_any_sync(FULL, l);
-        const bool leader = l != INVALID && lane == __ffs(peers) - 1;
-        double g = 0.0;
-        if (leader) g = gain_of(l, __popc(peers), deg, mine, st, p_ext, alpha);
-        // own community's gain -> remove gain
-        const unsigned own = __ballot_sync(FULL, leader && l == mine);
-        double remove_gain = 0.0;
-        {
-            double gm = __shfl_sync(FULL, g, own ? __ffs(own) - 1 : 0);
-            if (own) remove_gain = -gm;
-        }
-        // arg-max over positive gains
-        double bg = (leader && g > 0.0) ? g : 0.0;
-        uint32_t bl = (leader && g > 0.0) ? l : INVALID;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            double og = __shfl_xor_sync(FULL, bg, o);
-            uint32_t ol = __shfl_xor_sync(FULL, bl, o);
-            if (ol != INVALID && (bl == INVALID || better(og, ol, bg, bl))) {
-                bg = og;
-                bl = ol;
-            }
-        }
-        if (lane == 0) next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, remove_gain, mine);
-    }
-}
-
-// ---- degree > 32: one CTA per vertex, hash table of (label, count) --------
-
-__device__ __forceinline__ uint32_t hash32(uint32_t x) {
-    x ^= x >> 16;
-    x *= 0x7feb352du;
-    x ^= x >> 15;
-    x *= 0x846ca68bu;
-    x ^= x >> 16;
-    return x;
-}
-
-template <int THREADS>
-__device__ void improve_cta(uint32_t p, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
-                            const uint32_t *__restrict__ labels, const Stats &st, double p_ext, double alpha,
-                            uint32_t *next, uint32_t *keys, uint32_t *vals, uint32_t cap) {
-    __shared__ double s_gain[THREADS / 32];
-    __shared__ uint32_t s_label[THREADS / 32];
-    __shared__ double s_remove;
-    __shared__ int s_has_remove;
-    const uint32_t beg = indices[p], deg = indices[p + 1] - beg, mine = labels[p];
-    const uint32_t mask = cap - 1;
-    for (uint32_t i = threadIdx.x; i < cap; i += THREADS) {
-        keys[i] = INVALID;
-        vals[i] = 0;
-    }
-    if (threadIdx.x == 0) {
-        s_remove = 0.0;
-        s_has_remove = 0;
-    }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < deg; i += THREADS) {
-        const uint32_t l = labels[adj[beg + i]];
-        if (l == INVALID) continue;
-        uint32_t h = hash32(l) & mask;
-        while (true) {
-            uint32_t k = keys[h];
-            if (k == INVALID) {
-                k = atomicCAS(keys + h, INVALID, l);
-                if (k == INVALID) k = l;
-            }
-            if (k == l) {
-                atomicAdd(vals + h, 1u);
-                break;
-            }
-            h = (h + 1) & mask;
-        }
-    }
-    __syncthreads();
-    double bg = 0.0;
-    uint32_t bl = INVALID;
-    for (uint32_t i = threadIdx.x; i < cap; i += THREADS) {
-        const uint32_t l = keys[i];
-        if (l == INVALID) continue;
-        const double g = gain_of(l, vals[i], deg, mine, st, p_ext, alpha);
-        if (l == mine) {
-            s_remove = -g;
-            s_has_remove = 1;
-        }
-        if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
-            bg = g;
-            bl = l;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        double og = __shfl_xor_sync(FULL, bg, o);
-        uint32_t ol = __shfl_xor_sync(FULL, bl, o);
-        if (ol != INVALID && (bl == INVALID || better(og, ol, bg, bl))) {
-            bg = og;
-            bl = ol;
-        }
-    }
-    if ((threadIdx.x & 31) == 0) {
-        s_gain[threadIdx.x >> 5] = bg;
-        s_label[threadIdx.x >> 5] = bl;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < THREADS / 32; w++)
-            if (s_label[w] != INVALID && (bl == INVALID || better(s_gain[w], s_label[w], bg, bl))) {
-                bg = s_gain[w];
-                bl = s_label[w];
-            }
-        next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, s_has_remove ? s_remove : 0.0, mine);
-    }
-    __syncthreads();
-}
-
-constexpr int MID_THREADS = 256;
-constexpr uint32_t MID_CAP = 8192;   // shared-memory table entries (64 KB)
-
-__global__ void __launch_bounds__(MID_THREADS)
-k_improve_mid(const uint32_t *__restrict__ verts, uint32_t count, const uint32_t *__restrict__ indices,
-              const uint32_t *__restrict__ adj, const uint32_t *__restrict__ labels, Stats st,
-              const double *__restrict__ p_ext_ptr, double alpha, uint32_t *next) {
-    extern __shared__ uint32_t smem[];
-    uint32_t *keys = smem, *vals = smem + MID_CAP;
-    const double p_ext = *p_ext_ptr;
-    for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
-        const uint32_t p = verts[i];
-        const uint32_t deg = indices[p + 1] - indices[p];
-        uint32_t cap = 64;
-        while (cap < 2 * deg) cap <<= 1;
-        improve_cta<MID_THREADS>(p, indices, adj, labels, st, p_ext, alpha, next, keys, vals, cap);
-    }
-}
-
-__global__ void __launch_bounds__(MID_THREADS)
-k_improve_big(const uint32_t *__restrict__ verts, uint32_t count, const uint32_t *__restrict__ indices,
-              const uint32_t *__restrict__ adj, const uint32_t *__restrict__ labels, Stats st,
-              const double *__restrict__ p_ext_ptr, double alpha, uint32_t *next, uint32_t *tables,
-              const uint64_t *__restrict__ table_off) {
-    const double p_ext = *p_ext_ptr;
-    for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
-        const uint32_t p = verts[i];
-        const uint64_t off = table_off[i];
-        const uint32_t cap = (uint32_t)((table_off[i + 1] - off) / 2);
-        improve_cta<MID_THREADS>(p, indices, adj, labels, st, p_ext, alpha, next, tables + off, tables + off + cap,
-                                 cap);
-    }
-}
 
 // ---- collect_stats ---------------------------------------------------------
 
@@ -332,27 +127,125 @@ __global__ void k_pext_terms(uint32_t n, const uint32_t *__restrict__ indices, c
     }
 }
 
-// the reference's single-thread order (src/graph.cpp:59-68 at one thread):
-// ((t0 + t1) + t2) + ... over vertices with degree > 1, then / n
-__global__ void k_pext_sequential(uint32_t n, const uint32_t *__restrict__ indices, const double *__restrict__ term,
-                                  double *out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double s = 0.0;
-    uint32_t p = 0;
-    for (; p + 8 <= n; p += 8) {
-        double t[8];
-        uint32_t d[9];
-#pragma unroll
-        for (int k = 0; k < 9; k++) d[k] = indices[p + k];
-#pragma unroll
-        for (int k = 0; k < 8; k++) t[k] = term[p + k];
-#pragma unroll
-        for (int k = 0; k < 8; k++)
-            if (d[k + 1] - d[k] > 1) s = dadd(s, t[k]);
+// The reference's single-thread order (src/graph.cpp:59-68 at one thread),
+// s = ((t0 + t1) + t2) + ..., reproduced bit for bit without a 1.2M-long chain
+// of dependent FP64 adds (67 cycles each on GB300).  All terms are >= 0 (zero
+// for degree <= 1, which leaves s unchanged).  While s stays in one binade
+// [2^e, 2^(e+1)) it is an integer S times u = 2^(e-52), and fl(s + t) is
+// (S + round(t/u)) * u with round-to-nearest of the exact t/u — unless t/u has
+// a fractional part of exactly 1/2 (then ties-to-even depends on S) or the sum
+// leaves the binade.  So one CTA walks the terms in tiles of 8192: integer
+// roundings + a block prefix sum give every in-binade partial sum exactly, and
+// only the first tie or binade crossing in a tile is done with a real DADD,
+// after which the tile restarts from the next term.
+constexpr int SEQ_THREADS = 1024;
+constexpr int SEQ_ITEMS = 8;
+constexpr int SEQ_TILE = SEQ_THREADS * SEQ_ITEMS;
+
+__global__ void __launch_bounds__(SEQ_THREADS)
+k_sequential_sum_exact(const double *__restrict__ term, uint32_t n, double divisor, double *out) {
+    __shared__ long long warp_tot[SEQ_THREADS / 32];
+    __shared__ double s_val;
+    __shared__ uint32_t s_pos, s_event;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long TWO53 = 1ll << 53;
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        uint32_t p = 0;
+        while (p < n && s == 0.0) s = dadd(s, term[p++]);   // leading zero terms
+        s_val = s;
+        s_pos = p;
     }
-    for (; p < n; p++)
-        if (indices[p + 1] - indices[p] > 1) s = dadd(s, term[p]);
-    *out = ddiv(s, (double)n);
+    __syncthreads();
+    while (true) {
+        const uint32_t pos = s_pos;
+        if (pos >= n) break;
+        const double s = s_val;
+        if (!(s >= 2.2250738585072014e-308) || s > 1e300) {
+            // not a positive normal number (e.g. after a negative term): one plain step
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                s_val = dadd(s, term[pos]);
+                s_pos = pos + 1;
+            }
+            __syncthreads();
+            continue;
+        }
+        const int e = (int)((__double_as_longlong(s) >> 52) & 0x7ff) - 1023;   // s in [2^e, 2^(e+1))
+        const double scale = __longlong_as_double((long long)(1023 + 52 - e) << 52);   // 2^(52-e)
+        const double u = __longlong_as_double((long long)(1023 - 52 + e) << 52);       // 2^(e-52)
+        const long long S = __double2ll_rz(dmul(s, scale));
+        const uint32_t base = pos + threadIdx.x * SEQ_ITEMS;
+        long long r[SEQ_ITEMS];
+        bool ev[SEQ_ITEMS];
+        long long local = 0;
+#pragma unroll
+        for (int i = 0; i < SEQ_ITEMS; i++) {
+            r[i] = 0;
+            ev[i] = false;
+            if (base + i < n) {
+                const double x = dmul(term[base + i], scale);   // exact: power-of-two scaling
+                if (!(x >= 0.0) || x >= 9007199254740992.0) {
+                    ev[i] = true;
+                } else {
+                    const double q = floor(x), f = dsub(x, q);
+                    ev[i] = f == 0.5;
+                    r[i] = (long long)q + (f > 0.5 ? 1 : 0);
+                }
+            }
+            local += r[i];
+        }
+        // block exclusive scan of the per-thread totals
+        long long inc = local;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            long long v = __shfl_up_sync(FULL, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) warp_tot[warp] = inc;
+        if (threadIdx.x == 0) s_event = INVALID;
+        __syncthreads();
+        if (warp == 0) {
+            long long w = warp_tot[lane];
+            long long wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                long long v = __shfl_up_sync(FULL, wi, o);
+                if (lane >= o) wi += v;
+            }
+            warp_tot[lane] = wi - w;   // exclusive offset of each warp
+        }
+        __syncthreads();
+        long long run = S + warp_tot[warp] + (inc - local);   // value before this thread's first item
+        uint32_t first_event = INVALID;
+        long long before_event = 0;
+#pragma unroll
+        for (int i = 0; i < SEQ_ITEMS; i++) {
+            if (base + i < n && first_event == INVALID) {
+                if (ev[i] || run + r[i] >= TWO53) {
+                    first_event = base + i;
+                    before_event = run;
+                } else {
+                    run += r[i];
+                }
+            }
+        }
+        if (first_event != INVALID) atomicMin(&s_event, first_event);
+        __syncthreads();
+        const uint32_t evi = s_event;
+        if (evi == INVALID) {
+            const uint32_t last = min(n, pos + (uint32_t)SEQ_TILE) - 1;
+            if (last >= base && last < base + SEQ_ITEMS) {   // owner of the tile's last term
+                s_val = dmul((double)run, u);
+                s_pos = last + 1;
+            }
+        } else if (first_event == evi) {
+            s_val = dadd(dmul((double)before_event, u), term[evi]);
+            s_pos = evi + 1;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = ddiv(s_val, divisor);
 }
 
 __global__ void k_pext_tree(uint32_t n, const double *__restrict__ term, double *partial) {
@@ -380,34 +273,6 @@ void collect_stats(Ctx &c, const uint32_t *labels, Stats &st) {
     k_stats<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.adj, labels, st);
     CK_LAUNCH("k_stats");
     c.launches += 1;
-}
-
-void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next) {
-    const Graph &g = c.g;
-    cudaStream_t s = c.stream;
-    if (g.n == 0) return;
-    PhaseScope ph(c, "improve");
-    if (g.n_small) {
-        k_improve_warp<<<grid_for((uint64_t)g.n_small * 32, TPB), TPB, 0, s>>>(
-            g.cls_small, g.n_small, g.indices, g.adj, labels, st, g.p_ext_dev, c.alpha, next);
-        CK_LAUNCH("k_improve_warp");
-        c.launches++;
-    }
-    if (g.n_mid) {
-        const size_t smem = 2 * MID_CAP * sizeof(uint32_t);
-        CK(cudaFuncSetAttribute((const void *)k_improve_mid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_improve_mid<<<grid_for(g.n_mid, 1, 152 * 3), MID_THREADS, smem, s>>>(
-            g.cls_mid, g.n_mid, g.indices, g.adj, labels, st, g.p_ext_dev, c.alpha, next);
-        CK_LAUNCH("k_improve_mid");
-        c.launches++;
-    }
-    if (g.n_big) {
-        k_improve_big<<<grid_for(g.n_big, 1, 152 * 2), MID_THREADS, 0, s>>>(
-            g.cls_big, g.n_big, g.indices, g.adj, labels, st, g.p_ext_dev, c.alpha, next, c.big_tables,
-            g.big_table_off);
-        CK_LAUNCH("k_improve_big");
-        c.launches++;
-    }
 }
 
 void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
@@ -463,8 +328,8 @@ void compute_p_ext(Ctx &c) {
         CK_LAUNCH("k_wcc_final");
         c.launches += 2;
     } else {
-        k_pext_sequential<<<1, 32, 0, s>>>(g.n, g.indices, term.get(), g.p_ext_dev);
-        CK_LAUNCH("k_pext_sequential");
+        k_sequential_sum_exact<<<1, SEQ_THREADS, 0, s>>>(term.get(), g.n, (double)g.n, g.p_ext_dev);
+        CK_LAUNCH("k_sequential_sum_exact");
         c.launches += 1;
     }
     c.launches += 1;

@@ -156,11 +156,14 @@ def test_labels_to_device_roundtrip(engine):
     assert np.array_equal(engine.current_labels(), tr["labels"][3])
 
 
-def test_rmat16_full_pipeline_against_oracle(engine):
-    pairs = scdgen.rmat(16, 16, seed=22)
+@pytest.mark.parametrize("scale", [16, 18])
+def test_rmat_full_pipeline_against_oracle(engine, scale):
+    # scale 18: n = 104k, 13 tiles of the exact p_ext sum, hubs of degree ~25k
+    pairs = scdgen.rmat(scale, 16, seed=22)
     ref, _ = O.convert(pairs)
     engine.convert_edges(pairs)
     assert engine.graph_bytes() == ref.to_bytes()
+    assert engine.graph_info()[2] == O.clustering_coef(ref)
     r = O.run(ref, max_iters=50)
     engine.initial_partition()
     assert np.array_equal(engine.current_labels(), r["initial_labels"])
