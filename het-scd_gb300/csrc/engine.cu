@@ -156,8 +156,10 @@ void Ctx::free_all() {
     has_graph = has_labels = false;
     labels = labels_next = best = nullptr;
     st[0] = st[1] = Stats();
-    slot_cnt = nullptr;
-    itri = itdeg = nullptr;
+    slot_flag = nullptr;
+    itcount = nullptr;
+    itdeg = nullptr;
+    wplan = TcPlan();
     wcc_part = wcc_sum = nullptr;
     big_tables = nullptr;
     pin64 = nullptr;
@@ -198,9 +200,10 @@ void finish_graph(Ctx &c) {
     }
     c.pin64 = c.alloc<double>(n);
     c.pin32 = c.alloc<float2>(n);
-    c.slot_cnt = c.alloc<uint32_t>(2 * (size_t)g.m);
-    c.itri = c.alloc<int32_t>(n);
+    c.slot_flag = c.alloc<uint8_t>(2 * (size_t)g.m);
+    c.itcount = c.alloc<uint32_t>(n);
     c.itdeg = c.alloc<int32_t>(n);
+    if (n) tc_plan(c, Oriented{g.indices, g.nlow, g.adj, n}, c.wplan, s, true);
     c.wcc_part = c.alloc<double>((n + 2047) / 2048 + 1);
     c.wcc_sum = c.alloc<double>(1);
     compute_p_ext(c);

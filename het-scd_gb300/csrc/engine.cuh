@@ -21,10 +21,10 @@
 
 namespace scd {
 
-// vertex lists by degree: (0,8], (8,16], (16,32], (32,256], (256,4096], > 4096
+// vertex lists by degree: (0,8], (8,16], (16,32], (32,256], (256,2048], (2048,8192], > 8192
 struct DegreeClasses {
-    static constexpr int K = 6;
-    static constexpr uint32_t upper[K] = {8, 16, 32, 256, 4096, 0xffffffffu};
+    static constexpr int K = 7;
+    static constexpr uint32_t upper[K] = {8, 16, 32, 256, 2048, 8192, 0xffffffffu};
     uint32_t *list[K] = {};
     uint32_t count[K] = {};
 };
@@ -63,6 +63,28 @@ struct PhaseTimers {
     void destroy();
 };
 
+// triangles.cu: oriented triangle counting (per out-slot counters)
+struct Oriented {
+    const uint32_t *beg;   // out-list of u starts at beg[u]
+    const uint32_t *len;   // and has len[u] entries (sorted ascending by id)
+    const uint32_t *adj;
+    uint32_t n;
+};
+// out-degree buckets and their work-unit offsets (built once per oriented graph)
+struct TcPlan {
+    static constexpr int K = 4;
+    uint32_t *verts[K] = {};
+    uint32_t *unit_off[K] = {};
+    uint32_t nverts[K] = {};
+    DevBuf<uint32_t> tmp[2 * K];   // storage when the plan is temporary
+};
+struct Ctx;
+void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned);
+// tcount[v] += triangles at v; flag[slot] = 1 for out-slots on a triangle.
+// With labels: internal triangles only.  tcount and flag must be zeroed.
+void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, const uint32_t *labels, uint32_t *tcount,
+                     uint8_t *flag, cudaStream_t s);
+
 struct Ctx;
 // records [start, end) of a phase on the context's stream when profiling
 struct PhaseScope {
@@ -92,8 +114,10 @@ struct Ctx {
     int cur = 0;
     uint32_t num_comms = 0;
     bool has_labels = false;
-    uint32_t *slot_cnt = nullptr;
-    int32_t *itri = nullptr, *itdeg = nullptr;
+    uint8_t *slot_flag = nullptr;     // internal-triangle flag per adjacency position
+    uint32_t *itcount = nullptr;      // internal triangles per vertex
+    int32_t *itdeg = nullptr;         // edges on an internal triangle per vertex
+    TcPlan wplan;                     // triangle-counting plan of the resident graph
     double *wcc_part = nullptr, *wcc_sum = nullptr, *wcc_host = nullptr;
     uint32_t *big_tables = nullptr;   // global hash tables of the last degree bucket
     double *pin64 = nullptr;          // per-community p_in of the current statistics
@@ -122,15 +146,6 @@ void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const
                   const int32_t *tri, const int32_t *tri_deg);
 void finish_graph(Ctx &c);   // nlow, p_ext, degree classes, partition buffers
 
-// triangles.cu: oriented triangle counting (per out-slot counters)
-struct Oriented {
-    const uint32_t *beg;   // out-list of u starts at beg[u]
-    const uint32_t *len;   // and has len[u] entries (sorted ascending by id)
-    const uint32_t *adj;
-    uint32_t n;
-};
-void count_oriented_triangles(Ctx &c, const Oriented &o, const uint32_t *labels, uint32_t *slot_cnt,
-                              cudaStream_t s);
 
 // partition.cu
 void initial_partition(Ctx &c);

@@ -6,9 +6,9 @@
 //                    neighbour; __match_any_sync finds equal labels (groups
 //                    are separated by a lane mask), the lowest lane of each
 //                    equal-label set owns the label;
-//   33 .. 4096       one CTA per vertex, open-addressing hash table of
-//                    (label, count) in shared memory;
-//   > 4096           one CTA per vertex, per-vertex hash table in global memory.
+//   33 .. 8192       one CTA per vertex, open-addressing hash table of
+//                    (label, count) in shared memory (three sizes);
+//   > 8192           one CTA per vertex, per-vertex hash table in global memory.
 // Each distinct label other than p's own first gets an FP32 interval
 // enclosure of its FP64 gain (gain_interval.cuh).  The own label's gain (the
 // remove gain) is always evaluated exactly; a foreign label is evaluated
@@ -317,11 +317,15 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next) {
         c.launches++;
     }
     if (k.count[4]) {
-        launch_cta<256, 8192>(k.list[4], k.count[4], a, s, 152 * 3);
+        launch_cta<256, 4096>(k.list[4], k.count[4], a, s, 152 * 7);
         c.launches++;
     }
     if (k.count[5]) {
-        k_improve_global<<<grid_for(k.count[5], 1, 152 * 2), 256, 0, s>>>(k.list[5], k.count[5], a, c.big_tables,
+        launch_cta<512, 16384>(k.list[5], k.count[5], a, s, 152);
+        c.launches++;
+    }
+    if (k.count[6]) {
+        k_improve_global<<<grid_for(k.count[6], 1, 152 * 2), 256, 0, s>>>(k.list[6], k.count[6], a, c.big_tables,
                                                                          g.big_table_off);
         CK_LAUNCH("k_improve_global");
         c.launches++;

@@ -7,9 +7,9 @@
 //  2. both directions of every renamed non-loop pair as one 2k-bit key
 //     (row << k | col), one stable LSD radix sort, adjacent duplicates dropped:
 //     the de-duplicated symmetric CSR (src/convert.cpp:252-268 + 417-463);
-//  3. degree orientation (u -> v iff (deg v, v) > (deg u, u)) and per-out-slot
-//     triangle counts (triangles.cu); per vertex tri = sum of counts, tri_deg =
-//     number of edges with a count > 0 (src/convert.cpp:271-340);
+//  3. degree orientation (u -> v iff (deg v, v) > (deg u, u)), triangles per
+//     vertex and "edge lies on a triangle" flags (triangles.cu); tri = 2 x the
+//     vertex's triangles, tri_deg = number of flagged edges (src/convert.cpp:271-340);
 //  4. triangle-free edges dropped and vertices ranked by (tri_deg, id)
 //     descending, degree-0 vertices trimmed (src/convert.cpp:342-414);
 //  5. the final symmetric CSR by a second key sort (src/convert.cpp:417-455).
@@ -134,21 +134,22 @@ __global__ void k_out_ranges(const uint32_t *__restrict__ indices, const uint32_
     }
 }
 
-// tri[v] = sum of the counts of v's edges, tri_deg[v] = edges with count > 0
-// (src/convert.cpp:327-340; int32 wrap-around as in the reference)
-__global__ void k_vertex_triangles(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
-                                   const uint32_t *__restrict__ cnt, uint32_t count, int32_t *tri,
-                                   int32_t *tri_deg) {
+// tri_deg[v] = number of v's edges that lie on a triangle (src/convert.cpp:327-340)
+__global__ void k_flag_degrees(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
+                               const uint8_t *__restrict__ flag, uint32_t count, int32_t *tri_deg) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        uint32_t c = cnt[i];
-        if (c > 0) {
-            uint32_t u = orow[i], v = ocol[i];
-            atomicAdd((uint32_t *)tri + u, c);
-            atomicAdd((uint32_t *)tri + v, c);
-            atomicAdd(tri_deg + u, 1);
-            atomicAdd(tri_deg + v, 1);
+        if (flag[i]) {
+            atomicAdd(tri_deg + orow[i], 1);
+            atomicAdd(tri_deg + ocol[i], 1);
         }
     }
+}
+
+// tri[v] = sum of the per-edge counts at v = 2 x triangles at v, in int32
+// two's-complement arithmetic like the reference's int accumulator
+__global__ void k_tri_from_count(const uint32_t *__restrict__ tcount, uint32_t n, int32_t *tri) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        tri[v] = (int32_t)(2u * tcount[v]);
 }
 
 // key = ((2^32-1 - tri_deg) << k) | (2^k-1 - v): ascending = (tri_deg, v) descending
@@ -174,9 +175,9 @@ __global__ void k_rank_of(const uint32_t *__restrict__ order, uint32_t n, const 
     }
 }
 
-struct Positive {
-    const uint32_t *cnt;
-    __device__ uint32_t operator[](size_t i) const { return cnt[i] > 0; }
+struct Flagged {
+    const uint8_t *flag;
+    __device__ uint32_t operator[](size_t i) const { return flag[i] != 0; }
 };
 
 struct NonZeroDeg {
@@ -185,10 +186,10 @@ struct NonZeroDeg {
 };
 
 __global__ void k_final_keys(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
-                             const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ pos,
+                             const uint8_t *__restrict__ flag, const uint32_t *__restrict__ pos,
                              uint32_t count, const uint32_t *__restrict__ rank, int k, uint64_t *keys) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        if (cnt[i] > 0) {
+        if (flag[i]) {
             uint64_t a = rank[orow[i]], b = rank[ocol[i]];
             uint32_t o = pos[i];
             keys[2 * (uint64_t)o] = (a << k) | b;
@@ -274,7 +275,7 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
     // 3. degree orientation + triangle counts
     DevBuf<uint32_t> opos(slots1 + 1, s);
     scan_exclusive<uint32_t>(IsOut{rows1.get(), cols1.get(), ind1.get()}, opos.get(), slots1, s);
-    DevBuf<uint32_t> orow(m1, s), ocol(m1, s), obeg(n1, s), olen(n1, s), ocnt(m1, s);
+    DevBuf<uint32_t> orow(m1, s), ocol(m1, s), obeg(n1, s), olen(n1, s);
     k_orient<<<grid_for(slots1, TPB), TPB, 0, s>>>(rows1.get(), cols1.get(), ind1.get(), slots1, opos.get(),
                                                   orow.get(), ocol.get());
     CK_LAUNCH("k_orient");
@@ -284,15 +285,23 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
     rows1.release();
     cols1.release();
     ind1.release();
-    CK(cudaMemsetAsync(ocnt.get(), 0, (size_t)m1 * 4, s));
+    DevBuf<uint32_t> tcount(n1, s);
+    DevBuf<uint8_t> oflag(m1, s);
+    CK(cudaMemsetAsync(tcount.get(), 0, (size_t)n1 * 4, s));
+    CK(cudaMemsetAsync(oflag.get(), 0, m1, s));
     Oriented o{obeg.get(), olen.get(), ocol.get(), n1};
-    count_oriented_triangles(c, o, nullptr, ocnt.get(), s);
+    {
+        TcPlan plan;
+        tc_plan(c, o, plan, s, false);
+        count_triangles(c, o, plan, nullptr, tcount.get(), oflag.get(), s);
+    }
     DevBuf<int32_t> tri1(n1, s), tdeg1(n1, s);
-    CK(cudaMemsetAsync(tri1.get(), 0, (size_t)n1 * 4, s));
     CK(cudaMemsetAsync(tdeg1.get(), 0, (size_t)n1 * 4, s));
-    k_vertex_triangles<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), ocnt.get(), m1, tri1.get(),
-                                                        tdeg1.get());
-    CK_LAUNCH("k_vertex_triangles");
+    k_tri_from_count<<<grid_for(n1, TPB), TPB, 0, s>>>(tcount.get(), n1, tri1.get());
+    CK_LAUNCH("k_tri_from_count");
+    k_flag_degrees<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), oflag.get(), m1, tdeg1.get());
+    CK_LAUNCH("k_flag_degrees");
+    tcount.release();
     obeg.release();
     olen.release();
 
@@ -313,7 +322,7 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
 
     // 5. final symmetric CSR in rank ids
     DevBuf<uint32_t> fpos(m1 + 1, s);
-    scan_exclusive<uint32_t>(Positive{ocnt.get()}, fpos.get(), m1, s);
+    scan_exclusive<uint32_t>(Flagged{oflag.get()}, fpos.get(), m1, s);
     const uint32_t m2 = read_scalar(fpos.get() + m1, s);
 
     Graph &g = c.g;
@@ -329,7 +338,7 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
     if (m2 > 0) {
         const int k2 = ceil_log2(n2 < 2 ? 2 : n2);
         DevBuf<uint64_t> fkeys(2 * (size_t)m2, s);
-        k_final_keys<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), ocnt.get(), fpos.get(), m1,
+        k_final_keys<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), oflag.get(), fpos.get(), m1,
                                                       rank.get(), k2, fkeys.get());
         CK_LAUNCH("k_final_keys");
         radix_sort<uint64_t>(fkeys.get(), nullptr, 2 * (size_t)m2, 0, 2 * k2, s);

@@ -37,31 +37,23 @@ k_stats(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__rest
 
 // ---- WCC ---------------------------------------------------------------------
 
-// per-vertex sums of the internal per-edge triangle counts
+// int_tri_deg (src/wcc.cpp:124-126): per vertex, the internal edges that lie on an
+// internal triangle, counted from the out-slot flags of both endpoints
 __global__ void __launch_bounds__(TPB)
-k_internal_sums(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
-                const uint32_t *__restrict__ adj, const uint32_t *__restrict__ cnt, int32_t *itri,
-                int32_t *itdeg) {
+k_internal_degrees(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
+                   const uint32_t *__restrict__ adj, const uint8_t *__restrict__ flag, int32_t *itdeg) {
     const int lane = threadIdx.x & 31;
     for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += (gridDim.x * blockDim.x) >> 5) {
         const uint32_t beg = indices[u], len = nlow[u];
-        uint32_t sum = 0, edges = 0;
+        uint32_t edges = 0;
         for (uint32_t i = lane; i < len; i += 32) {
-            const uint32_t c = cnt[beg + i];
-            if (c) {
-                const uint32_t v = adj[beg + i];
-                atomicAdd((uint32_t *)itri + v, c);
-                atomicAdd(itdeg + v, 1);
-                sum += c;
+            if (flag[beg + i]) {
+                atomicAdd(itdeg + adj[beg + i], 1);
                 edges++;
             }
         }
-        sum = warp_sum(sum);
         edges = warp_sum(edges);
-        if (lane == 0 && edges) {
-            atomicAdd((uint32_t *)itri + u, sum);
-            atomicAdd(itdeg + u, (int)edges);
-        }
+        if (lane == 0 && edges) atomicAdd(itdeg + u, (int)edges);
     }
 }
 
@@ -70,13 +62,13 @@ constexpr int WCC_CHUNK = TPB * WCC_ITEMS;
 
 // WCC_p of src/wcc.cpp:129-134
 __device__ __forceinline__ double wcc_term(uint32_t p, const uint32_t *labels, const Stats &st,
-                                           const int32_t *tri, const int32_t *tri_deg, const int32_t *itri,
+                                           const int32_t *tri, const int32_t *tri_deg, const uint32_t *itcount,
                                            const int32_t *itdeg, double alpha) {
     const uint32_t l = labels[p];
     if (l == INVALID) return 0.0;
     const int size = st.sizes[l], td = tri_deg[p];
     if (size <= 2 || td == 0) return 0.0;
-    const int it = itri[p], itd = itdeg[p];
+    const int it = (int)(2u * itcount[p]), itd = itdeg[p];   // int_tri = 2 x internal triangles
     const double nom = (double)imul_wrap(it, td);
     const double den = dmul((double)tri[p], dadd((double)td, dmul(alpha, (double)(size - 1 - itd))));
     return den != 0.0 ? ddiv(nom, den) : 0.0;
@@ -96,14 +88,14 @@ __device__ __forceinline__ double block_sum_fixed(double v, double *sh) {
 
 __global__ void __launch_bounds__(TPB)
 k_wcc_partial(uint32_t n, const uint32_t *__restrict__ labels, Stats st, const int32_t *__restrict__ tri,
-              const int32_t *__restrict__ tri_deg, const int32_t *__restrict__ itri,
+              const int32_t *__restrict__ tri_deg, const uint32_t *__restrict__ itcount,
               const int32_t *__restrict__ itdeg, double alpha, double *partial) {
     __shared__ double sh[TPB / 32];
     const uint32_t base = blockIdx.x * WCC_CHUNK + threadIdx.x * WCC_ITEMS;
     double s = 0.0;
 #pragma unroll
     for (int i = 0; i < WCC_ITEMS; i++)
-        if (base + i < n) s = dadd(s, wcc_term(base + i, labels, st, tri, tri_deg, itri, itdeg, alpha));
+        if (base + i < n) s = dadd(s, wcc_term(base + i, labels, st, tri, tri_deg, itcount, itdeg, alpha));
     double r = block_sum_fixed(s, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = r;
 }
@@ -283,16 +275,16 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
         return;
     }
     PhaseScope ph(c, "wcc");
-    CK(cudaMemsetAsync(c.slot_cnt, 0, 2 * (size_t)g.m * 4, s));
-    CK(cudaMemsetAsync(c.itri, 0, (size_t)g.n * 4, s));
+    CK(cudaMemsetAsync(c.slot_flag, 0, 2 * (size_t)g.m, s));
+    CK(cudaMemsetAsync(c.itcount, 0, (size_t)g.n * 4, s));
     CK(cudaMemsetAsync(c.itdeg, 0, (size_t)g.n * 4, s));
     Oriented o{g.indices, g.nlow, g.adj, g.n};
-    count_oriented_triangles(c, o, labels, c.slot_cnt, s);
-    k_internal_sums<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj, c.slot_cnt,
-                                                                     c.itri, c.itdeg);
-    CK_LAUNCH("k_internal_sums");
+    count_triangles(c, o, c.wplan, labels, c.itcount, c.slot_flag, s);
+    k_internal_degrees<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj,
+                                                                        c.slot_flag, c.itdeg);
+    CK_LAUNCH("k_internal_degrees");
     const uint32_t parts = (g.n + WCC_CHUNK - 1) / WCC_CHUNK;
-    k_wcc_partial<<<parts, TPB, 0, s>>>(g.n, labels, st, g.tri, g.tri_deg, c.itri, c.itdeg, c.alpha, c.wcc_part);
+    k_wcc_partial<<<parts, TPB, 0, s>>>(g.n, labels, st, g.tri, g.tri_deg, c.itcount, c.itdeg, c.alpha, c.wcc_part);
     CK_LAUNCH("k_wcc_partial");
     k_wcc_final<<<1, TPB, 0, s>>>(c.wcc_part, parts, g.n, c.wcc_sum);
     CK_LAUNCH("k_wcc_final");

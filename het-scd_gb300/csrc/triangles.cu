@@ -1,78 +1,108 @@
-// Triangle counting on a degree-oriented graph, with per-edge counters.
+// Triangle counting on a degree-oriented graph: per-vertex triangle counts and
+// per-edge "lies on a triangle" flags.
 //
-// Every undirected edge has one out-slot (in the out-list of its lower-ranked
-// endpoint).  A triangle {a, b, c} with a -> b, a -> c, b -> c is found once,
-// from a: for b in out(a), every c in out(b) ∩ out(a) adds 1 to the counters of
-// the three slots (a,b), (a,c), (b,c).  The per-edge totals are exactly the
-// per-edge triangle counts t[e] of the reference's merge over the id-oriented
-// list (src/convert.cpp:290-319), computed with O(sum d+(a) d+(b)) work instead
-// of the reference's id orientation, whose hubs make it quadratic.
+// Every undirected edge has one out-slot in the out-list of its lower-ranked
+// endpoint.  A triangle {a, b, c} with a -> b, a -> c, b -> c is found once,
+// from a: for b in out(a), every c in out(b) ∩ out(a).  That is all the
+// reference's outputs need (src/convert.cpp:290-340): tri[v] = sum of the
+// per-edge counts at v = 2 x (triangles at v), and tri_deg[v] and the filter
+// need only whether an edge's count is > 0.  So the kernel produces
+//   tcount[v]  triangles at v (tri = 2 tcount),
+//   flag[slot] 1 if the edge of that out-slot lies on a triangle,
+// and never a per-edge counter: a's and b's counts and the (a,b), (a,c) flags
+// are aggregated in shared memory per work unit; the only per-triangle global
+// write is the byte store flag(b,c) = 1 (idempotent, no atomic).
+// The reference's id-oriented merge is quadratic in hub degree; this does
+// sum over a->b of d+(b) hash probes.
 //
-// With labels, only internal triangles count (all three vertices share a valid
-// label): the per-edge internal counts that compute_wcc derives by merging each
-// vertex's same-label neighbours (src/wcc.cpp:84-127), and that the reference
-// GPU path gets from a compacted internal CSR (src/cuda.cu:285-330,
-// src/kernels.cuh:299-356).
+// With labels, only internal triangles count (all three vertices carry the
+// same valid label): compute_wcc's int_tri = 2 tcount and int_tri_deg = number
+// of flagged edges (src/wcc.cpp:84-127).
 //
-// Work decomposition: a unit is (vertex a, 32 consecutive entries b of out(a)).
-// Units are handed to warps dynamically (heavy out-lists are split across
-// warps).  out(a) is staged in the warp's shared memory; the warp flattens the
-// items (b, c in out(b)) of its 32 b's with a prefix sum, each lane takes items
-// and looks c up in out(a) by binary search.
+// Work unit = (vertex a, up to 32 consecutive b of out(a)) for one warp, or
+// (a, up to 256 b) for one CTA when out(a) is long.  out(a) is staged in a
+// shared-memory open-addressing table (load <= 1/4 for short lists); the
+// unit's items (b, c in out(b)) are flattened with a prefix sum and each thread
+// walks 8 consecutive items; a one-hash bitmap (>= 16 bits per entry) in front
+// of the table answers most lookups, which are misses, with one shared load.  Units are grouped by the out-degree of a into
+// buckets so each kernel's shared memory matches its lists.
 #include "engine.cuh"
 
 namespace scd {
 
 namespace {
 
-constexpr int TC_WARPS = 8;
-constexpr int TC_THREADS = TC_WARPS * 32;
-constexpr int TC_STAGE = 1024;   // out-list entries staged per warp
+constexpr uint32_t EMPTY = 0xffffffffu;
+constexpr int ITEMS = 8;   // consecutive items per thread
+
+constexpr uint32_t HASH_MUL = 0x9E3779B1u;   // multiplicative hash: table index = top bits
 
 struct UnitsOf {
-    const uint32_t *len;
-    const uint32_t *labels;
-    __device__ uint32_t operator[](size_t a) const {
-        if (labels && labels[a] == INVALID) return 0;
-        return (len[a] + 31) >> 5;
-    }
+    const uint32_t *verts, *len;
+    uint32_t per_unit;
+    __device__ uint32_t operator[](size_t i) const { return (len[verts[i]] + per_unit - 1) / per_unit; }
 };
 
-__global__ void __launch_bounds__(TC_THREADS)
-k_tc_units(Oriented o, const uint32_t *__restrict__ labels, const uint32_t *__restrict__ unit_off,
-           uint32_t *slot_cnt, uint32_t *next_unit) {
-    __shared__ uint32_t stage[TC_WARPS][TC_STAGE];
-    __shared__ uint32_t pre[TC_WARPS][32];
-    __shared__ uint32_t bbase[TC_WARPS][32];
-    __shared__ uint32_t bhits[TC_WARPS][32];
+struct InBucket {
+    const uint32_t *len;
+    uint32_t lo, hi;
+    __device__ uint32_t operator[](size_t v) const { return len[v] > lo && len[v] <= hi; }
+};
+
+__global__ void k_bucket_scatter(uint32_t n, InBucket f, const uint32_t *__restrict__ pos, uint32_t *out) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        if (f[v]) out[pos[v]] = v;
+}
+
+// Warp units.  Per warp: table of TCAP (key, index) entries, LCAP counters.
+template <int WARPS, int TCAP, int LCAP, int FBITS>
+__global__ void __launch_bounds__(WARPS * 32)
+k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off, uint32_t nverts,
+          const uint32_t *__restrict__ labels, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+    __shared__ uint32_t filt[WARPS][(1 << FBITS) / 32];
+    __shared__ uint32_t keys[WARPS][TCAP];
+    __shared__ uint16_t idxs[WARPS][TCAP];
+    __shared__ uint32_t cnt[WARPS][LCAP];
+    __shared__ uint32_t pre[WARPS][32], bbase[WARPS][32], bhits[WARPS][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const uint32_t n_units = unit_off[o.n];
+    const uint32_t n_units = unit_off[nverts];
     while (true) {
         uint32_t unit = 0;
         if (lane == 0) unit = atomicAdd(next_unit, 1u);
         unit = __shfl_sync(FULL, unit, 0);
         if (unit >= n_units) break;
-        // vertex a: unit_off[a] <= unit < unit_off[a+1]
-        uint32_t lo = 0, hi = o.n + 1;
+        uint32_t lo = 0, hi = nverts + 1;   // vertex index: unit_off[i] <= unit < unit_off[i+1]
         while (lo < hi) {
-            uint32_t mid = (lo + hi) >> 1;
+            const uint32_t mid = (lo + hi) >> 1;
             if (unit_off[mid] <= unit) lo = mid + 1;
             else hi = mid;
         }
-        const uint32_t a = lo - 1;
-        const uint32_t ch = unit - unit_off[a];
+        const uint32_t vi = lo - 1;
+        const uint32_t a = verts[vi], ch = unit - unit_off[vi];
         const uint32_t la = labels ? labels[a] : 0u;
+        if (labels && la == INVALID) continue;
         const uint32_t abeg = o.beg[a], alen = o.len[a];
-        const bool staged = alen <= TC_STAGE;
-        if (staged)
-            for (uint32_t i = lane; i < alen; i += 32) stage[w][i] = o.adj[abeg + i];
+        int bits = 1;
+        while ((1u << bits) < 4 * alen) bits++;
+        if ((1 << bits) > TCAP) bits = 31 - __clz(TCAP);
+        const uint32_t tmask = (1u << bits) - 1;
+        for (uint32_t i = lane; i < (1u << bits); i += 32) keys[w][i] = EMPTY;
+        for (uint32_t i = lane; i < (1u << FBITS) / 32; i += 32) filt[w][i] = 0;
+        for (uint32_t i = lane; i < alen; i += 32) cnt[w][i] = 0;
         __syncwarp();
-        const uint32_t *A = staged ? stage[w] : o.adj + abeg;
-
+        for (uint32_t i = lane; i < alen; i += 32) {
+            const uint32_t id = o.adj[abeg + i];
+            const uint32_t hv = id * HASH_MUL, fi = hv >> (32 - FBITS);
+            atomicOr(&filt[w][fi >> 5], 1u << (fi & 31));
+            uint32_t h = hv >> (32 - bits);
+            while (atomicCAS(&keys[w][h], EMPTY, id) != EMPTY) h = (h + 1) & tmask;
+            idxs[w][h] = (uint16_t)i;
+        }
+        __syncwarp();
         const uint32_t j = ch * 32 + lane;
-        uint32_t wb = 0, bb = 0;
+        uint32_t wb = 0, bb = 0, b = 0;
         if (j < alen) {
-            uint32_t b = A[j];
+            b = o.adj[abeg + j];
             if (!labels || labels[b] == la) {
                 wb = o.len[b];
                 bb = o.beg[b];
@@ -84,44 +114,312 @@ k_tc_units(Oriented o, const uint32_t *__restrict__ labels, const uint32_t *__re
         bbase[w][lane] = bb;
         bhits[w][lane] = 0;
         __syncwarp();
-        for (uint32_t t = lane; t < total; t += 32) {
-            // owner lane of item t: last lane with pre <= t
-            uint32_t l0 = 0, l1 = 32;
+        for (uint32_t t0 = lane * ITEMS; t0 < total; t0 += 32 * ITEMS) {
+            uint32_t l0 = 0, l1 = 32;   // owner lane of t0: last lane with pre <= t0
             while (l0 < l1) {
-                uint32_t mid = (l0 + l1) >> 1;
-                if (pre[w][mid] <= t) l0 = mid + 1;
+                const uint32_t mid = (l0 + l1) >> 1;
+                if (pre[w][mid] <= t0) l0 = mid + 1;
                 else l1 = mid;
             }
-            const uint32_t jb = l0 - 1;
-            const uint32_t cpos = bbase[w][jb] + (t - pre[w][jb]);
-            const uint32_t c = o.adj[cpos];
-            const uint32_t ic = lower_bound(A, alen, c);
-            bool hit = ic < alen && A[ic] == c;
-            if (hit && labels) hit = labels[c] == la;
-            if (hit) {
-                atomicAdd(&bhits[w][jb], 1u);
-                atomicAdd(slot_cnt + abeg + ic, 1u);
-                atomicAdd(slot_cnt + cpos, 1u);
+            uint32_t jb = l0 - 1;
+            uint32_t nxt = jb + 1 < 32 ? pre[w][jb + 1] : total;
+            uint32_t cbase = bbase[w][jb] - pre[w][jb];
+            uint32_t cpos[ITEMS], cv[ITEMS], own[ITEMS];
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                const uint32_t t = t0 + k;
+                own[k] = INVALID;
+                if (t < total) {
+                    while (t >= nxt) {
+                        jb++;
+                        nxt = jb + 1 < 32 ? pre[w][jb + 1] : total;
+                        cbase = bbase[w][jb] - pre[w][jb];
+                    }
+                    own[k] = jb;
+                    cpos[k] = cbase + t;
+                    cv[k] = o.adj[cpos[k]];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                if (own[k] == INVALID) continue;
+                const uint32_t c = cv[k];
+                const uint32_t hv = c * HASH_MUL, fi = hv >> (32 - FBITS);
+                if (!((filt[w][fi >> 5] >> (fi & 31)) & 1u)) continue;   // certainly not in out(a)
+                uint32_t h = hv >> (32 - bits), key;
+                while ((key = keys[w][h]) != c && key != EMPTY) h = (h + 1) & tmask;
+                if (key == c && (!labels || labels[c] == la)) {
+                    atomicAdd(&cnt[w][idxs[w][h]], 1u);
+                    atomicAdd(&bhits[w][own[k]], 1u);
+                    flag[cpos[k]] = 1;
+                }
             }
         }
         __syncwarp();
-        if (j < alen && bhits[w][lane]) atomicAdd(slot_cnt + abeg + j, bhits[w][lane]);
+        const uint32_t hb = j < alen ? bhits[w][lane] : 0;
+        if (hb) {
+            atomicAdd(tcount + b, hb);
+            flag[abeg + j] = 1;
+        }
+        const uint32_t sa = warp_sum(hb);
+        if (lane == 0 && sa) atomicAdd(tcount + a, sa);
+        for (uint32_t i = lane; i < alen; i += 32) {
+            const uint32_t cc = cnt[w][i];
+            if (cc) {
+                atomicAdd(tcount + o.adj[abeg + i], cc);
+                flag[abeg + i] = 1;
+            }
+        }
         __syncwarp();
     }
 }
 
+// CTA units for longer out-lists: (a, up to THREADS b), one shared table per CTA.
+template <int THREADS, int TCAP, int LCAP, int FBITS>
+__global__ void __launch_bounds__(THREADS)
+k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off, uint32_t nverts,
+         const uint32_t *__restrict__ labels, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+    extern __shared__ uint32_t sm[];
+    uint32_t *keys = sm;                                  // TCAP
+    uint32_t *cnt = sm + TCAP;                            // LCAP
+    uint32_t *filt = sm + TCAP + LCAP;                    // 2^FBITS bits
+    uint16_t *idxs = (uint16_t *)(filt + (1 << FBITS) / 32);   // TCAP
+    __shared__ uint32_t pre[THREADS], bbase[THREADS], bhits[THREADS], wsum[THREADS / 32];
+    __shared__ uint32_t s_unit, s_total;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t n_units = unit_off[nverts];
+    while (true) {
+        if (threadIdx.x == 0) s_unit = atomicAdd(next_unit, 1u);
+        __syncthreads();
+        const uint32_t unit = s_unit;
+        if (unit >= n_units) break;
+        uint32_t lo = 0, hi = nverts + 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (unit_off[mid] <= unit) lo = mid + 1;
+            else hi = mid;
+        }
+        const uint32_t vi = lo - 1;
+        const uint32_t a = verts[vi], ch = unit - unit_off[vi];
+        const uint32_t la = labels ? labels[a] : 0u;
+        if (labels && la == INVALID) {
+            __syncthreads();
+            continue;
+        }
+        const uint32_t abeg = o.beg[a], alen = o.len[a];
+        int bits = 1;
+        while ((1u << bits) < 2 * alen) bits++;
+        const uint32_t tmask = (1u << bits) - 1;
+        for (uint32_t i = threadIdx.x; i < (1u << bits); i += THREADS) keys[i] = EMPTY;
+        for (uint32_t i = threadIdx.x; i < (1u << FBITS) / 32; i += THREADS) filt[i] = 0;
+        for (uint32_t i = threadIdx.x; i < alen; i += THREADS) cnt[i] = 0;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < alen; i += THREADS) {
+            const uint32_t id = o.adj[abeg + i];
+            const uint32_t hv = id * HASH_MUL, fi = hv >> (32 - FBITS);
+            atomicOr(&filt[fi >> 5], 1u << (fi & 31));
+            uint32_t h = hv >> (32 - bits);
+            while (atomicCAS(&keys[h], EMPTY, id) != EMPTY) h = (h + 1) & tmask;
+            idxs[h] = (uint16_t)i;
+        }
+        const uint32_t j = ch * THREADS + threadIdx.x;
+        uint32_t wb = 0, bb = 0, b = 0;
+        if (j < alen) {
+            b = o.adj[abeg + j];
+            if (!labels || labels[b] == la) {
+                wb = o.len[b];
+                bb = o.beg[b];
+            }
+        }
+        uint32_t incl = warp_inclusive_scan(wb);   // block inclusive scan of wb
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int k = 0; k < THREADS / 32; k++) {
+                const uint32_t x = wsum[k];
+                wsum[k] = run;
+                run += x;
+            }
+            s_total = run;
+        }
+        __syncthreads();
+        incl += wsum[w];
+        pre[threadIdx.x] = incl - wb;
+        bbase[threadIdx.x] = bb;
+        bhits[threadIdx.x] = 0;
+        const uint32_t total = s_total;
+        __syncthreads();
+        // each thread walks ITEMS consecutive items: one owner search, independent loads
+        for (uint32_t t0 = threadIdx.x * ITEMS; t0 < total; t0 += THREADS * ITEMS) {
+            uint32_t l0 = 0, l1 = THREADS;   // owner of t0: last thread with pre <= t0
+            while (l0 < l1) {
+                const uint32_t mid = (l0 + l1) >> 1;
+                if (pre[mid] <= t0) l0 = mid + 1;
+                else l1 = mid;
+            }
+            uint32_t jb = l0 - 1;
+            uint32_t nxt = jb + 1 < THREADS ? pre[jb + 1] : total;
+            uint32_t cbase = bbase[jb] - pre[jb];
+            uint32_t cpos[ITEMS], cv[ITEMS], own[ITEMS];
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                const uint32_t t = t0 + k;
+                own[k] = INVALID;
+                if (t < total) {
+                    while (t >= nxt) {
+                        jb++;
+                        nxt = jb + 1 < THREADS ? pre[jb + 1] : total;
+                        cbase = bbase[jb] - pre[jb];
+                    }
+                    own[k] = jb;
+                    cpos[k] = cbase + t;
+                    cv[k] = o.adj[cpos[k]];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                if (own[k] == INVALID) continue;
+                const uint32_t c = cv[k];
+                const uint32_t hv = c * HASH_MUL, fi = hv >> (32 - FBITS);
+                if (!((filt[fi >> 5] >> (fi & 31)) & 1u)) continue;   // certainly not in out(a)
+                uint32_t h = hv >> (32 - bits), key;
+                while ((key = keys[h]) != c && key != EMPTY) h = (h + 1) & tmask;
+                if (key == c && (!labels || labels[c] == la)) {
+                    atomicAdd(&cnt[idxs[h]], 1u);
+                    atomicAdd(&bhits[own[k]], 1u);
+                    flag[cpos[k]] = 1;
+                }
+            }
+        }
+        __syncthreads();
+        const uint32_t hb = j < alen ? bhits[threadIdx.x] : 0;
+        if (hb) {
+            atomicAdd(tcount + b, hb);
+            flag[abeg + j] = 1;
+        }
+        const uint32_t sa = warp_sum(hb);
+        if (lane == 0 && sa) atomicAdd(tcount + a, sa);
+        for (uint32_t i = threadIdx.x; i < alen; i += THREADS) {
+            const uint32_t cc = cnt[i];
+            if (cc) {
+                atomicAdd(tcount + o.adj[abeg + i], cc);
+                flag[abeg + i] = 1;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int THREADS, int TCAP, int LCAP, int FBITS>
+void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, const uint32_t *labels, uint32_t *tcount,
+                   uint8_t *flag, uint32_t *ctr, unsigned grid, cudaStream_t s) {
+    const size_t smem = (size_t)TCAP * 4 + (size_t)LCAP * 4 + ((size_t)1 << FBITS) / 8 + (size_t)TCAP * 2;
+    if (smem > 48 * 1024)
+        CK(cudaFuncSetAttribute((const void *)k_tc_cta<THREADS, TCAP, LCAP, FBITS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_tc_cta<THREADS, TCAP, LCAP, FBITS><<<grid, THREADS, smem, s>>>(o, plan.verts[k], plan.unit_off[k], plan.nverts[k],
+                                                            labels, tcount, flag, ctr);
+    CK_LAUNCH("k_tc_cta");
+}
+
+// Lists longer than 8192 (none in the benchmark graphs): items looked up
+// by binary search in the sorted out-list in global memory, per-triangle
+// atomics.  Kept for generality.
+__global__ void __launch_bounds__(256)
+k_tc_huge(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, const uint32_t *__restrict__ labels,
+          uint32_t *tcount, uint8_t *flag) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t vi = 0; vi < nverts; vi++) {
+        const uint32_t a = verts[vi];
+        const uint32_t la = labels ? labels[a] : 0u;
+        if (labels && la == INVALID) continue;
+        const uint32_t abeg = o.beg[a], alen = o.len[a];
+        const uint32_t *A = o.adj + abeg;
+        for (uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < alen; j += warps) {
+            const uint32_t b = A[j];
+            if (labels && labels[b] != la) continue;
+            const uint32_t bbeg = o.beg[b], blen = o.len[b];
+            uint32_t hits = 0;
+            for (uint32_t i = lane; i < blen; i += 32) {
+                const uint32_t c = o.adj[bbeg + i];
+                const uint32_t ic = lower_bound(A, alen, c);
+                if (ic < alen && A[ic] == c && (!labels || labels[c] == la)) {
+                    hits++;
+                    atomicAdd(tcount + c, 1u);
+                    flag[abeg + ic] = 1;
+                    flag[bbeg + i] = 1;
+                }
+            }
+            hits = warp_sum(hits);
+            if (lane == 0 && hits) {
+                atomicAdd(tcount + a, hits);
+                atomicAdd(tcount + b, hits);
+                flag[abeg + j] = 1;
+            }
+        }
+    }
+}
+
+// out-degree buckets: (0,64] warp units, (64,1024] and (1024,8192] CTA units, > 8192 fallback
+constexpr uint32_t B0 = 64, B1 = 1024, B2 = 8192;
+
 }  // namespace
 
-void count_oriented_triangles(Ctx &c, const Oriented &o, const uint32_t *labels, uint32_t *slot_cnt,
-                              cudaStream_t s) {
+void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned) {
+    const uint32_t bounds[TcPlan::K + 1] = {0, B0, B1, B2, 0xffffffffu};
+    const uint32_t per_unit[TcPlan::K] = {32, 128, 256, 1};
+    for (int k = 0; k < TcPlan::K; k++) {
+        DevBuf<uint32_t> pos((size_t)o.n + 1, s);
+        InBucket f{o.len, bounds[k], bounds[k + 1]};
+        scan_exclusive<uint32_t>(f, pos.get(), o.n, s);
+        uint32_t cnt = 0;
+        CK(cudaMemcpyAsync(&cnt, pos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        plan.nverts[k] = cnt;
+        if (owned) {
+            plan.verts[k] = c.alloc<uint32_t>(cnt);
+            plan.unit_off[k] = c.alloc<uint32_t>((size_t)cnt + 1);
+        } else {
+            plan.tmp[2 * k].alloc(cnt ? cnt : 1, s);
+            plan.tmp[2 * k + 1].alloc((size_t)cnt + 1, s);
+            plan.verts[k] = plan.tmp[2 * k].get();
+            plan.unit_off[k] = plan.tmp[2 * k + 1].get();
+        }
+        if (cnt) {
+            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, f, pos.get(), plan.verts[k]);
+            CK_LAUNCH("k_bucket_scatter");
+        }
+        scan_exclusive<uint32_t>(UnitsOf{plan.verts[k], o.len, per_unit[k]}, plan.unit_off[k], cnt, s);
+    }
+}
+
+void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, const uint32_t *labels, uint32_t *tcount,
+                     uint8_t *flag, cudaStream_t s) {
     if (o.n == 0) return;
-    DevBuf<uint32_t> unit_off((size_t)o.n + 1, s);
-    scan_exclusive<uint32_t>(UnitsOf{o.len, labels}, unit_off.get(), o.n, s);
-    CK(cudaMemsetAsync(c.work_counter, 0, 4, s));
     PhaseScope ph(c, labels ? "wcc_tc" : "tc");
-    k_tc_units<<<152 * 4, TC_THREADS, 0, s>>>(o, labels, unit_off.get(), slot_cnt, c.work_counter);
-    CK_LAUNCH("k_tc_units");
-    c.launches += 3;
+    uint32_t *ctr = c.work_counter;
+    CK(cudaMemsetAsync(ctr, 0, 16, s));
+    if (plan.nverts[0]) {
+        k_tc_warp<16, 256, 64, 10><<<152 * 4, 16 * 32, 0, s>>>(o, plan.verts[0], plan.unit_off[0], plan.nverts[0],
+                                                           labels, tcount, flag, ctr);
+        CK_LAUNCH("k_tc_warp64");
+        c.launches++;
+    }
+    if (plan.nverts[1]) {
+        launch_tc_cta<128, 2048, 1024, 14>(o, plan, 1, labels, tcount, flag, ctr + 1, 152 * 12, s);
+        c.launches++;
+    }
+    if (plan.nverts[2]) {
+        launch_tc_cta<256, 16384, 8192, 17>(o, plan, 2, labels, tcount, flag, ctr + 2, 152, s);
+        c.launches++;
+    }
+    if (plan.nverts[3]) {
+        k_tc_huge<<<152 * 4, 256, 0, s>>>(o, plan.verts[3], plan.nverts[3], labels, tcount, flag);
+        CK_LAUNCH("k_tc_huge");
+        c.launches++;
+    }
 }
 
 }  // namespace scd
