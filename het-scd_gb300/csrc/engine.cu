@@ -41,7 +41,7 @@ struct TableWords {
         const uint64_t d = indices[v + 1] - indices[v];
         uint64_t cap = 64;
         while (cap < 2 * d) cap <<= 1;
-        return 2 * cap;
+        return 3 * cap;   // keys, counts, occupied-entry list
     }
 };
 

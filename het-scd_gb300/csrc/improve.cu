@@ -150,13 +150,17 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     return x;
 }
 
+// One vertex per CTA.  keys/vals is an open-addressing table of cap (label,
+// count) entries; list receives the index of every occupied entry, so both
+// passes touch only the distinct labels.
 template <int THREADS>
-__device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, uint32_t *vals, uint32_t cap,
-                            double p_ext, Iv pe, Iv al) {
+__device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, uint32_t *vals, uint32_t *list,
+                            uint32_t cap, double p_ext, Iv pe, Iv al) {
     __shared__ double s_gain[THREADS / 32];
     __shared__ uint32_t s_label[THREADS / 32];
     __shared__ float s_lo[THREADS / 32];
     __shared__ double s_remove;
+    __shared__ uint32_t s_n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t beg = a.indices[p], deg = a.indices[p + 1] - beg, mine = a.labels[p];
     const uint32_t mask = cap - 1;
@@ -164,7 +168,10 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
         keys[i] = INVALID;
         vals[i] = 0;
     }
-    if (threadIdx.x == 0) s_remove = 0.0;
+    if (threadIdx.x == 0) {
+        s_remove = 0.0;
+        s_n = 0;
+    }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < deg; i += THREADS) {
         const uint32_t l = a.labels[a.adj[beg + i]];
@@ -174,7 +181,10 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
             uint32_t k = keys[h];
             if (k == INVALID) {
                 k = atomicCAS(keys + h, INVALID, l);
-                if (k == INVALID) k = l;
+                if (k == INVALID) {
+                    list[atomicAdd(&s_n, 1u)] = h;   // first occurrence of l
+                    k = l;
+                }
             }
             if (k == l) {
                 atomicAdd(vals + h, 1u);
@@ -184,18 +194,15 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
         }
     }
     __syncthreads();
-    // pass 1: own gain (exact) and the best lower bound among foreign labels
+    const uint32_t nl = s_n;
+    // pass 1: best lower bound among foreign labels
     float m = -INFINITY;
-    for (uint32_t i = threadIdx.x; i < cap; i += THREADS) {
-        const uint32_t l = keys[i];
-        if (l == INVALID) continue;
-        if (l == mine) {
-            s_remove = -exact_gain(a, l, vals[i], deg, mine, p_ext);
-        } else {
-            bool need = false;
-            const Iv iv = interval_gain(a, l, vals[i], deg, pe, al, &need);
-            if (!need) m = fmaxf(m, iv.lo);
-        }
+    for (uint32_t i = threadIdx.x; i < nl; i += THREADS) {
+        const uint32_t h = list[i], l = keys[h];
+        if (l == mine) continue;
+        bool need = false;
+        const Iv iv = interval_gain(a, l, vals[h], deg, pe, al, &need);
+        if (!need) m = fmaxf(m, iv.lo);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
@@ -204,16 +211,19 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     m = s_lo[0];
 #pragma unroll
     for (int w = 1; w < THREADS / 32; w++) m = fmaxf(m, s_lo[w]);
-    // pass 2: exact gains of the surviving labels
+    // pass 2: exact gains of the own label (remove gain) and of the survivors
     double bg = 0.0;
     uint32_t bl = INVALID;
-    for (uint32_t i = threadIdx.x; i < cap; i += THREADS) {
-        const uint32_t l = keys[i];
-        if (l == INVALID || l == mine) continue;
+    for (uint32_t i = threadIdx.x; i < nl; i += THREADS) {
+        const uint32_t h = list[i], l = keys[h];
+        if (l == mine) {
+            s_remove = -exact_gain(a, l, vals[h], deg, mine, p_ext);
+            continue;
+        }
         bool need = false;
-        const Iv iv = interval_gain(a, l, vals[i], deg, pe, al, &need);
+        const Iv iv = interval_gain(a, l, vals[h], deg, pe, al, &need);
         if (need || (iv.hi > 0.f && iv.hi >= m)) {
-            const double g = exact_gain(a, l, vals[i], deg, mine, p_ext);
+            const double g = exact_gain(a, l, vals[h], deg, mine, p_ext);
             if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
                 bg = g;
                 bl = l;
@@ -249,7 +259,7 @@ template <int THREADS, uint32_t CAP>
 __global__ void __launch_bounds__(THREADS)
 k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
     extern __shared__ uint32_t smem[];
-    uint32_t *keys = smem, *vals = smem + CAP;
+    uint32_t *keys = smem, *vals = smem + CAP, *list = smem + 2 * CAP;
     const double p_ext = *a.p_ext_ptr;
     const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
@@ -257,25 +267,29 @@ k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a)
         const uint32_t deg = a.indices[p + 1] - a.indices[p];
         uint32_t cap = 64;
         while (cap < 2 * deg) cap <<= 1;
-        improve_cta<THREADS>(a, p, keys, vals, cap, p_ext, pe, al);
+        improve_cta<THREADS>(a, p, keys, vals, list, cap, p_ext, pe, al);
     }
 }
 
-__global__ void __launch_bounds__(256)
+constexpr int GLOBAL_THREADS = 512;
+
+// tables: per vertex 3*cap words (keys, counts, occupied-entry list)
+__global__ void __launch_bounds__(GLOBAL_THREADS)
 k_improve_global(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a, uint32_t *tables,
                  const uint64_t *__restrict__ table_off) {
     const double p_ext = *a.p_ext_ptr;
     const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
         const uint64_t off = table_off[i];
-        const uint32_t cap = (uint32_t)((table_off[i + 1] - off) / 2);
-        improve_cta<256>(a, verts[i], tables + off, tables + off + cap, cap, p_ext, pe, al);
+        const uint32_t cap = (uint32_t)((table_off[i + 1] - off) / 3);
+        uint32_t *t = tables + off;
+        improve_cta<GLOBAL_THREADS>(a, verts[i], t, t + cap, t + 2 * cap, cap, p_ext, pe, al);
     }
 }
 
 template <int THREADS, uint32_t CAP>
 void launch_cta(const uint32_t *verts, uint32_t count, const ImproveArgs &a, cudaStream_t s, unsigned max_grid) {
-    const size_t smem = 2 * CAP * sizeof(uint32_t);
+    const size_t smem = (2 * CAP + CAP / 2) * sizeof(uint32_t);
     if (smem > 48 * 1024)
         CK(cudaFuncSetAttribute((const void *)k_improve_cta<THREADS, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem));
@@ -325,8 +339,8 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next) {
         c.launches++;
     }
     if (k.count[6]) {
-        k_improve_global<<<grid_for(k.count[6], 1, 152 * 2), 256, 0, s>>>(k.list[6], k.count[6], a, c.big_tables,
-                                                                         g.big_table_off);
+        k_improve_global<<<grid_for(k.count[6], 1, 152 * 2), GLOBAL_THREADS, 0, s>>>(k.list[6], k.count[6], a,
+                                                                                    c.big_tables, g.big_table_off);
         CK_LAUNCH("k_improve_global");
         c.launches++;
     }

@@ -141,7 +141,7 @@ __global__ void k_reduce_max(const T *in, size_t n, T *out) {
 
 constexpr int RS_WARPS = 8;
 constexpr int RS_THREADS = RS_WARPS * 32;
-constexpr int RS_ITEMS = 16;
+constexpr int RS_ITEMS = 8;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 
 template <typename K>
@@ -171,18 +171,24 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const K *keys, size_t
     }
 }
 
+// Ranks every key of the tile stably by digit, reorders the tile in shared
+// memory, then writes it out in tile order so that keys of one digit leave as
+// one contiguous run (coalesced) at the digit's global offset.
 template <typename K, bool HAS_VALS>
-__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *keys_in, const uint32_t *vals_in,
-                                                             K *keys_out, uint32_t *vals_out,
-                                                             size_t n, int shift, unsigned mask,
-                                                             const uint32_t *offsets, size_t tiles) {
+__global__ void __launch_bounds__(RS_THREADS, 4) k_rs_downsweep(const K *keys_in, const uint32_t *vals_in,
+                                                                K *keys_out, uint32_t *vals_out,
+                                                                size_t n, int shift, unsigned mask,
+                                                                const uint32_t *offsets, size_t tiles) {
     __shared__ uint32_t cnt[RS_WARPS][256];
-    __shared__ uint32_t base_of[256];
+    __shared__ uint32_t tile_start[256];   // first tile position of each digit
+    __shared__ uint32_t glob[256];         // global position of that first key
+    __shared__ K skeys[RS_TILE];
+    __shared__ uint32_t svals[HAS_VALS ? RS_TILE : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < RS_WARPS * 256; i += RS_THREADS) (&cnt[0][0])[i] = 0;
-    for (int d = threadIdx.x; d < 256; d += RS_THREADS) base_of[d] = offsets[(size_t)d * tiles + blockIdx.x];
     __syncthreads();
-    const size_t base = (size_t)blockIdx.x * RS_TILE + (size_t)warp * 32 * RS_ITEMS;
+    const size_t tile_base = (size_t)blockIdx.x * RS_TILE;
+    const size_t base = tile_base + (size_t)warp * 32 * RS_ITEMS;
     K key[RS_ITEMS];
     uint32_t val[RS_ITEMS];
     uint32_t rank[RS_ITEMS];
@@ -206,15 +212,27 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *keys_in, c
         __syncwarp();
     }
     __syncthreads();
-    // per digit: exclusive prefix over warps, then add the tile's global base
-    for (int d = threadIdx.x; d < 256; d += RS_THREADS) {
-        uint32_t run = base_of[d];
+    // per digit: exclusive prefix over warps (in place) and the digit's tile total
+    uint32_t total = 0;
+    if (threadIdx.x < 256) {
+        const int d = threadIdx.x;
 #pragma unroll
         for (int w = 0; w < RS_WARPS; w++) {
             uint32_t c = cnt[w][d];
-            cnt[w][d] = run;
-            run += c;
+            cnt[w][d] = total;
+            total += c;
         }
+        glob[d] = offsets[(size_t)d * tiles + blockIdx.x];
+    }
+    // exclusive scan of the 256 digit totals (RS_THREADS == 256: one per thread)
+    {
+        __shared__ uint32_t wsum[RS_WARPS];
+        uint32_t inc = warp_inclusive_scan(total);
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        uint32_t off = 0;
+        for (int w = 0; w < warp; w++) off += wsum[w];
+        tile_start[threadIdx.x] = off + inc - total;
     }
     __syncthreads();
 #pragma unroll
@@ -222,10 +240,19 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(const K *keys_in, c
         size_t idx = base + (size_t)k * 32 + lane;
         if (idx < n) {
             unsigned d = (unsigned)(key[k] >> shift) & mask;
-            uint32_t dst = cnt[warp][d] + rank[k];
-            keys_out[dst] = key[k];
-            if (HAS_VALS) vals_out[dst] = val[k];
+            uint32_t p = tile_start[d] + cnt[warp][d] + rank[k];
+            skeys[p] = key[k];
+            if (HAS_VALS) svals[p] = val[k];
         }
+    }
+    __syncthreads();
+    const uint32_t count = (uint32_t)min((size_t)RS_TILE, n - tile_base);
+    for (uint32_t i = threadIdx.x; i < count; i += RS_THREADS) {
+        const K kk = skeys[i];
+        const unsigned d = (unsigned)(kk >> shift) & mask;
+        const uint32_t dst = glob[d] + (i - tile_start[d]);
+        keys_out[dst] = kk;
+        if (HAS_VALS) vals_out[dst] = svals[i];
     }
 }
 

@@ -22,8 +22,9 @@
 // Work unit = (vertex a, up to 32 consecutive b of out(a)) for one warp, or
 // (a, up to 256 b) for one CTA when out(a) is long.  out(a) is staged in a
 // shared-memory open-addressing table (load <= 1/4 for short lists); the
-// unit's items (b, c in out(b)) are flattened with a prefix sum and each thread
-// walks 8 consecutive items; a one-hash bitmap (>= 16 bits per entry) in front
+// unit's items (b, c in out(b)) are flattened with a prefix sum; a warp takes
+// 256 consecutive items, lane L every 32nd from L (coalesced loads), walking
+// the b boundaries forward; a one-hash bitmap (>= 16 bits per entry) in front
 // of the table answers most lookups, which are misses, with one shared load.  Units are grouped by the out-degree of a into
 // buckets so each kernel's shared memory matches its lists.
 #include "engine.cuh"
@@ -114,11 +115,12 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
         bbase[w][lane] = bb;
         bhits[w][lane] = 0;
         __syncwarp();
-        for (uint32_t t0 = lane * ITEMS; t0 < total; t0 += 32 * ITEMS) {
-            uint32_t l0 = 0, l1 = 32;   // owner lane of t0: last lane with pre <= t0
+        for (uint32_t t0 = 0; t0 < total; t0 += 32 * ITEMS) {
+            const uint32_t tl = t0 + lane;   // lane L takes items t0 + L + 32k (coalesced)
+            uint32_t l0 = 0, l1 = 32;        // owner lane of tl: last lane with pre <= tl
             while (l0 < l1) {
                 const uint32_t mid = (l0 + l1) >> 1;
-                if (pre[w][mid] <= t0) l0 = mid + 1;
+                if (pre[w][mid] <= tl) l0 = mid + 1;
                 else l1 = mid;
             }
             uint32_t jb = l0 - 1;
@@ -127,7 +129,7 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
             uint32_t cpos[ITEMS], cv[ITEMS], own[ITEMS];
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
-                const uint32_t t = t0 + k;
+                const uint32_t t = tl + 32 * k;
                 own[k] = INVALID;
                 if (t < total) {
                     while (t >= nxt) {
@@ -250,12 +252,14 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
         bhits[threadIdx.x] = 0;
         const uint32_t total = s_total;
         __syncthreads();
-        // each thread walks ITEMS consecutive items: one owner search, independent loads
-        for (uint32_t t0 = threadIdx.x * ITEMS; t0 < total; t0 += THREADS * ITEMS) {
-            uint32_t l0 = 0, l1 = THREADS;   // owner of t0: last thread with pre <= t0
+        // warp chunks of 32*ITEMS consecutive items; lane L takes items chunk + L + 32k
+        // (coalesced loads) and walks the owner boundaries forward
+        for (uint32_t t0 = (uint32_t)w * 32 * ITEMS; t0 < total; t0 += THREADS * ITEMS) {
+            const uint32_t tl = t0 + lane;
+            uint32_t l0 = 0, l1 = THREADS;   // owner of tl: last thread with pre <= tl
             while (l0 < l1) {
                 const uint32_t mid = (l0 + l1) >> 1;
-                if (pre[mid] <= t0) l0 = mid + 1;
+                if (pre[mid] <= tl) l0 = mid + 1;
                 else l1 = mid;
             }
             uint32_t jb = l0 - 1;
@@ -264,7 +268,7 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
             uint32_t cpos[ITEMS], cv[ITEMS], own[ITEMS];
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
-                const uint32_t t = t0 + k;
+                const uint32_t t = tl + 32 * k;
                 own[k] = INVALID;
                 if (t < total) {
                     while (t >= nxt) {
