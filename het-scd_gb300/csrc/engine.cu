@@ -1,4 +1,5 @@
 // Context management, per-graph setup and the C ABI (include/scd_gb300.h).
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <new>
@@ -44,6 +45,54 @@ struct TableWords {
         return 3 * cap;   // keys, counts, occupied-entry list
     }
 };
+
+__global__ void k_seen_labels(uint32_t n, const uint32_t *__restrict__ labels, uint32_t nc, uint32_t *seen) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t l = labels[v];
+        if (l != INVALID && l < nc) seen[l] = 1;
+    }
+}
+
+__global__ void k_distinct_per_graph(uint32_t G, const uint32_t *__restrict__ comm_off, const uint32_t *__restrict__ scan,
+                                     uint32_t *out) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x)
+        out[g] = scan[comm_off[g + 1]] - scan[comm_off[g]];
+}
+
+__global__ void k_local_graph(uint32_t n_g, uint32_t m2_g, uint32_t v0, const uint32_t *__restrict__ indices,
+                              const uint32_t *__restrict__ adj, uint32_t *ind_out, uint32_t *adj_out) {
+    const uint32_t e0 = indices[v0];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n_g; i += gridDim.x * blockDim.x)
+        ind_out[i] = indices[v0 + i] - e0;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < m2_g; j += gridDim.x * blockDim.x)
+        adj_out[j] = adj[e0 + j] - v0;
+}
+
+__global__ void k_local_labels(uint32_t n_g, uint32_t v0, uint32_t l0, const uint32_t *__restrict__ labels,
+                               uint32_t *out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_g; i += gridDim.x * blockDim.x) {
+        const uint32_t l = labels[v0 + i];
+        out[i] = l == INVALID ? INVALID : l - l0;
+    }
+}
+
+__global__ void k_gather_indices(uint32_t G, const uint32_t *__restrict__ fin_off, const uint32_t *__restrict__ indices,
+                                 uint32_t *out) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x)
+        out[g] = indices[fin_off[g]];
+}
+
+__global__ void k_fill_gid(uint32_t n, uint32_t G, const uint32_t *__restrict__ fin_off, uint32_t *gid) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = G + 1;   // last g with fin_off[g] <= v
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (fin_off[mid] <= v) lo = mid + 1;
+            else hi = mid;
+        }
+        gid[v] = lo - 1;
+    }
+}
 
 __global__ void k_mark_labels(uint32_t n, const uint32_t *__restrict__ labels, uint32_t *seen, uint32_t nc) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -129,7 +178,7 @@ void PhaseTimers::destroy() {
 }
 
 PhaseScope::PhaseScope(Ctx &ctx, const char *name) : c(&ctx), idx(-1) {
-    if (!(ctx.flags & SCD_FLAG_PROFILE)) return;
+    if (!(ctx.flags & SCD_FLAG_PROFILE) || ctx.capturing) return;
     idx = ctx.timers.index(name);
     start = ctx.timers.get_event();
     CK(cudaEventRecord(start, ctx.stream));
@@ -160,7 +209,8 @@ void Ctx::free_all() {
     itcount = nullptr;
     itdeg = nullptr;
     wplan = TcPlan();
-    wcc_part = wcc_sum = nullptr;
+    wcc_part = nullptr;
+    b = Batch();
     big_tables = nullptr;
     pin64 = nullptr;
     pin32 = nullptr;
@@ -172,7 +222,55 @@ void finish_graph(Ctx &c) {
     cudaStream_t s = c.stream;
     const uint32_t n = g.n;
     g.nlow = c.alloc<uint32_t>(n);
-    g.p_ext_dev = c.alloc<double>(1);
+    prepare_tc_kernels();
+    prepare_improve_kernels();
+    // per-graph bookkeeping of the (possibly one-graph) batch
+    Batch &b = c.b;
+    if (!b.fin_off) {
+        b.fin_off = c.alloc<uint32_t>(b.G + 1);
+        CK(cudaMemcpyAsync(b.fin_off, b.h_fin_off.data(), 4 * (b.G + 1), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));   // h_fin_off is complete
+    {
+        std::vector<uint32_t> ind_at(b.G + 1);
+        DevBuf<uint32_t> tmp(b.G + 1, s);
+        k_gather_indices<<<grid_for(b.G + 1, TPB), TPB, 0, s>>>(b.G, b.fin_off, g.indices, tmp.get());
+        CK_LAUNCH("k_gather_indices");
+        CK(cudaMemcpyAsync(ind_at.data(), tmp.get(), 4 * (b.G + 1), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        b.h_m.resize(b.G);
+        for (uint32_t k = 0; k < b.G; k++) b.h_m[k] = (ind_at[k + 1] - ind_at[k]) / 2;
+    }
+    if (b.G > 1) {
+        b.gid = c.alloc<uint32_t>(n);
+        if (n) {
+            k_fill_gid<<<grid_for(n, TPB), TPB, 0, s>>>(n, b.G, b.fin_off, b.gid);
+            CK_LAUNCH("k_fill_gid");
+        }
+    }
+    {
+        std::vector<uint32_t> blk_off(b.G + 1, 0), blk_gid;
+        for (uint32_t k = 0; k < b.G; k++) {
+            const uint32_t nk = b.h_fin_off[k + 1] - b.h_fin_off[k];
+            const uint32_t parts = (nk + 2047) / 2048;
+            blk_off[k + 1] = blk_off[k] + parts;
+            blk_gid.insert(blk_gid.end(), parts, k);
+        }
+        b.blocks = blk_off[b.G];
+        b.blk_off = c.alloc<uint32_t>(b.G + 1);
+        b.blk_gid = c.alloc<uint32_t>(b.blocks);
+        CK(cudaMemcpyAsync(b.blk_off, blk_off.data(), 4 * (b.G + 1), cudaMemcpyHostToDevice, s));
+        if (b.blocks) CK(cudaMemcpyAsync(b.blk_gid, blk_gid.data(), 4 * b.blocks, cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    b.p_ext = c.alloc<double>(b.G);
+    b.comm_off = c.alloc<uint32_t>(b.G + 1);
+    b.wcc = c.alloc<double>(b.G);
+    b.best_wcc = c.alloc<double>(b.G);
+    b.active = c.alloc<uint8_t>(b.G);
+    b.improved = c.alloc<uint8_t>(b.G);
+    b.iters = c.alloc<int32_t>(b.G);
+    b.n_active = c.alloc<uint32_t>(1);
     if (n) {
         k_nlow<<<grid_for(n, TPB), TPB, 0, s>>>(n, g.indices, g.adj, g.nlow);
         CK_LAUNCH("k_nlow");
@@ -204,8 +302,7 @@ void finish_graph(Ctx &c) {
     c.itcount = c.alloc<uint32_t>(n);
     c.itdeg = c.alloc<int32_t>(n);
     if (n) tc_plan(c, Oriented{g.indices, g.nlow, g.adj, n}, c.wplan, s, true);
-    c.wcc_part = c.alloc<double>((n + 2047) / 2048 + 1);
-    c.wcc_sum = c.alloc<double>(1);
+    c.wcc_part = c.alloc<double>(b.blocks + 1);
     compute_p_ext(c);
     c.launches += 4;
 }
@@ -263,6 +360,9 @@ void set_labels(Ctx &c, const uint32_t *host_labels) {
     CK(cudaStreamSynchronize(s));
     if (nc > g.n) throw Error(SCD_ERR_ARG, "labels must be < n or SCD_INVALID_LABEL");
     c.num_comms = nc;
+    c.b.h_comm_off.assign(c.b.G + 1, nc);
+    c.b.h_comm_off[0] = 0;
+    CK(cudaMemcpyAsync(c.b.comm_off, c.b.h_comm_off.data(), 4 * (c.b.G + 1), cudaMemcpyHostToDevice, s));
     c.cur = 0;
     collect_stats(c, c.labels, c.st[0]);
     if (g.n) CK(cudaMemcpyAsync(c.best, c.labels, (size_t)g.n * 4, cudaMemcpyDeviceToDevice, s));
@@ -280,6 +380,124 @@ double iterate(Ctx &c) {
     return compute_wcc(c, c.labels, c.st[c.cur]);
 }
 
+double now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// One refinement iteration for every graph still running, without host
+// synchronisation (so it can be captured in a CUDA graph): improve, statistics,
+// WCC, per-graph loop control.
+void iterate_async(Ctx &c, double threshold, double *trace, int max_trace) {
+    improve(c, c.labels, c.st[c.cur], c.labels_next, c.b.G > 1);
+    uint32_t *t = c.labels;
+    c.labels = c.labels_next;
+    c.labels_next = t;
+    c.cur ^= 1;
+    collect_stats(c, c.labels, c.st[c.cur]);
+    launch_wcc(c, c.labels, c.st[c.cur]);
+    batch_step(c, threshold, trace, max_trace);
+}
+
+struct RunOut {
+    std::vector<double> wcc0, best;
+    std::vector<int32_t> iters;
+    std::vector<uint8_t> active;
+    std::vector<uint32_t> distinct;
+    double ms_partition = 0, ms_iterations = 0;
+};
+
+// number of distinct valid labels of each graph (compress_labels prints n - that)
+std::vector<uint32_t> distinct_per_graph(Ctx &c, const uint32_t *labels) {
+    Batch &b = c.b;
+    cudaStream_t s = c.stream;
+    std::vector<uint32_t> out(b.G, 0);
+    if (c.g.n == 0 || c.num_comms == 0) return out;
+    DevBuf<uint32_t> seen(c.num_comms, s), scan((size_t)c.num_comms + 1, s), dg(b.G, s);
+    CK(cudaMemsetAsync(seen.get(), 0, (size_t)c.num_comms * 4, s));
+    k_seen_labels<<<grid_for(c.g.n, TPB), TPB, 0, s>>>(c.g.n, labels, c.num_comms, seen.get());
+    CK_LAUNCH("k_seen_labels");
+    scan_exclusive<uint32_t>((const uint32_t *)seen.get(), scan.get(), c.num_comms, s);
+    k_distinct_per_graph<<<grid_for(b.G, TPB), TPB, 0, s>>>(b.G, b.comm_off, scan.get(), dg.get());
+    CK_LAUNCH("k_distinct_per_graph");
+    CK(cudaMemcpyAsync(out.data(), dg.get(), 4 * b.G, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    c.launches += 3;
+    return out;
+}
+
+// The loop of src/main-gpu.cpp:54-95 for every graph of the context at once;
+// each iteration is replayed from a captured CUDA graph (two graphs, one per
+// parity of the label double buffer), with one host read per iteration.
+void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int max_trace, RunOut &out) {
+    Batch &b = c.b;
+    cudaStream_t s = c.stream;
+    const double t0 = now_ms();
+    if (!c.has_labels) initial_partition(c);
+    launch_wcc(c, c.labels, c.st[c.cur]);
+    batch_reset(c);
+    out.wcc0.resize(b.G);
+    CK(cudaMemcpyAsync(out.wcc0.data(), b.wcc, 8 * b.G, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const double t1 = now_ms();
+    const bool graphs = !(c.flags & SCD_FLAG_PROFILE) && c.g.n > 0;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    try {
+        for (int it = 0; it < max_iters; it++) {
+            if (graphs) {
+                const int par = c.cur;
+                if (!exec[par]) {
+                    cudaGraph_t gr = nullptr;
+                    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                    c.capturing = true;
+                    try {
+                        iterate_async(c, threshold, trace_dev, max_trace);
+                    } catch (...) {
+                        c.capturing = false;
+                        cudaStreamEndCapture(s, &gr);
+                        if (gr) cudaGraphDestroy(gr);
+                        throw;
+                    }
+                    c.capturing = false;
+                    CK(cudaStreamEndCapture(s, &gr));
+                    const cudaError_t e = cudaGraphInstantiate(&exec[par], gr, 0);
+                    cudaGraphDestroy(gr);
+                    CK(e);
+                } else {
+                    // replaying advances the state exactly as the captured host code did
+                    uint32_t *t = c.labels;
+                    c.labels = c.labels_next;
+                    c.labels_next = t;
+                    c.cur ^= 1;
+                }
+                CK(cudaGraphLaunch(exec[par], s));
+                c.launches += 12;
+            } else {
+                iterate_async(c, threshold, trace_dev, max_trace);
+            }
+            CK(cudaMemcpyAsync(c.host_u32, b.n_active, 4, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (*c.host_u32 == 0) break;
+        }
+    } catch (...) {
+        for (auto e : exec)
+            if (e) cudaGraphExecDestroy(e);
+        throw;
+    }
+    for (auto e : exec)
+        if (e) cudaGraphExecDestroy(e);
+    const double t2 = now_ms();
+    out.best.resize(b.G);
+    out.iters.resize(b.G);
+    out.active.resize(b.G);
+    CK(cudaMemcpyAsync(out.best.data(), b.best_wcc, 8 * b.G, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out.iters.data(), b.iters, 4 * b.G, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(out.active.data(), b.active, b.G, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    out.distinct = distinct_per_graph(c, c.best);
+    out.ms_partition = t1 - t0;
+    out.ms_iterations = t2 - t1;
+}
+
 uint32_t distinct_labels(Ctx &c, const uint32_t *labels) {
     const Graph &g = c.g;
     cudaStream_t s = c.stream;
@@ -295,9 +513,6 @@ uint32_t distinct_labels(Ctx &c, const uint32_t *labels) {
     return cnt;
 }
 
-double now_ms() {
-    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
-}
 
 }  // namespace
 
@@ -320,6 +535,7 @@ int scd_create(scd_ctx **out, int device_id, int work_group_size, unsigned flags
         CK(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
         CK(cudaMalloc((void **)&c.work_counter, 64));
         CK(cudaMallocHost((void **)&c.wcc_host, sizeof(double)));
+        CK(cudaMallocHost((void **)&c.host_u32, 2 * sizeof(uint32_t)));
     } catch (const Error &e) {
         scd_destroy(ctx);
         return e.status;
@@ -335,6 +551,7 @@ void scd_destroy(scd_ctx *ctx) {
     c.free_all();
     if (c.work_counter) cudaFree(c.work_counter);
     if (c.wcc_host) cudaFreeHost(c.wcc_host);
+    if (c.host_u32) cudaFreeHost(c.host_u32);
     c.timers.destroy();
     if (c.stream) cudaStreamDestroy(c.stream);
     if (c.side) cudaStreamDestroy(c.side);
@@ -465,38 +682,128 @@ int scd_community_stats(scd_ctx *ctx, int32_t *sizes, int32_t *ext, int32_t *int
 int scd_run(scd_ctx *ctx, double threshold, int max_iters, double *wcc_trace, scd_result *res) {
     return guarded(ctx, [&](Ctx &c) {
         require_graph(c);
+        if (c.b.G != 1) throw Error(SCD_ERR_STATE, "the context holds a batch: use scd_batch_run");
+        if (max_iters < 0) throw Error(SCD_ERR_ARG, "max_iters < 0");
+        DevBuf<double> trace(wcc_trace && max_iters ? max_iters : 0, c.stream);
+        RunOut o;
+        run_loop(c, threshold, max_iters, trace.get(), wcc_trace ? max_iters : 0, o);
         scd_result r;
         memset(&r, 0, sizeof r);
-        double t0 = now_ms();
-        if (!c.has_labels) initial_partition(c);
-        r.initial_communities = c.num_comms;
-        double best_wcc = compute_wcc(c, c.labels, c.st[c.cur]);
-        r.initial_wcc = best_wcc;
-        double t1 = now_ms();
-        bool converged = false;
-        int iters = 0;
-        while (iters < max_iters) {
-            iters++;
-            double w = iterate(c);
-            if (w > best_wcc && c.g.n)
-                CK(cudaMemcpyAsync(c.best, c.labels, (size_t)c.g.n * 4, cudaMemcpyDeviceToDevice, c.stream));
-            if (wcc_trace) wcc_trace[iters - 1] = w;
-            if (w < best_wcc * (1 + threshold)) {
-                converged = true;
-                break;
-            }
-            best_wcc = w;
+        r.iterations = o.iters[0];
+        r.initial_wcc = o.wcc0[0];
+        r.best_wcc = o.best[0];
+        r.initial_communities = c.b.h_comm_off[1] - c.b.h_comm_off[0];
+        r.distinct_communities = o.distinct[0];
+        r.printed_communities = c.g.n - o.distinct[0];
+        r.ms_partition = o.ms_partition;
+        r.ms_iterations = o.ms_iterations;
+        if (wcc_trace && r.iterations > 0) {
+            CK(cudaMemcpyAsync(wcc_trace, trace.get(), 8 * std::min(r.iterations, max_iters), cudaMemcpyDeviceToHost,
+                               c.stream));
+            CK(cudaStreamSynchronize(c.stream));
+        }
+        if (res) *res = r;
+        if (o.active[0] || (c.g.n == 0 && max_iters > 0))
+            throw Error(SCD_ERR_LIMIT, "max_iters reached before convergence (or the WCC stays 0)");
+    });
+}
+
+int scd_batch_convert(scd_ctx *ctx, const uint32_t *pairs, const uint64_t *record_offsets, uint32_t num_graphs,
+                      int pairs_on_device) {
+    return guarded(ctx, [&](Ctx &c) {
+        if (!record_offsets || num_graphs == 0) throw Error(SCD_ERR_ARG, "no graphs");
+        std::vector<uint64_t> off(record_offsets, record_offsets + num_graphs + 1);
+        for (uint32_t g = 0; g < num_graphs; g++)
+            if (off[g + 1] < off[g]) throw Error(SCD_ERR_ARG, "record_offsets must be non-decreasing");
+        if (off[0] != 0) throw Error(SCD_ERR_ARG, "record_offsets[0] must be 0");
+        const uint64_t count = off[num_graphs];
+        if (count && !pairs) throw Error(SCD_ERR_ARG, "pairs is NULL");
+        if (pairs_on_device || count == 0) {
+            convert_edges(c, pairs, count, &off);
+        } else {
+            DevBuf<uint32_t> d(2 * count, c.stream);
+            CK(cudaMemcpyAsync(d.get(), pairs, 2 * count * 4, cudaMemcpyHostToDevice, c.stream));
+            convert_edges(c, d.get(), count, &off);
         }
         CK(cudaStreamSynchronize(c.stream));
-        double t2 = now_ms();
-        r.iterations = iters;
-        r.best_wcc = best_wcc;
-        r.distinct_communities = distinct_labels(c, c.best);
-        r.printed_communities = c.g.n - r.distinct_communities;
-        r.ms_partition = t1 - t0;
-        r.ms_iterations = t2 - t1;
-        if (res) *res = r;
-        if (!converged) throw Error(SCD_ERR_LIMIT, "max_iters reached before convergence");
+    });
+}
+
+int scd_batch_size(scd_ctx *ctx, uint32_t *num_graphs) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_graph(c);
+        if (num_graphs) *num_graphs = c.b.G;
+    });
+}
+
+int scd_batch_graph_info(scd_ctx *ctx, uint32_t g, uint32_t *n, uint32_t *m, double *cc) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_graph(c);
+        if (g >= c.b.G) throw Error(SCD_ERR_ARG, "graph index out of range");
+        if (n) *n = c.b.h_fin_off[g + 1] - c.b.h_fin_off[g];
+        if (m) *m = c.b.h_m[g];
+        if (cc) *cc = c.b.h_p_ext[g];
+    });
+}
+
+int scd_batch_graph_download(scd_ctx *ctx, uint32_t g, uint32_t *indices, uint32_t *adj, int32_t *tri,
+                             int32_t *tri_deg) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_graph(c);
+        if (g >= c.b.G) throw Error(SCD_ERR_ARG, "graph index out of range");
+        cudaStream_t s = c.stream;
+        const uint32_t v0 = c.b.h_fin_off[g], ng = c.b.h_fin_off[g + 1] - v0, m2 = 2 * c.b.h_m[g];
+        DevBuf<uint32_t> ind((size_t)ng + 1, s), ad(m2 ? m2 : 1, s);
+        k_local_graph<<<grid_for((uint64_t)ng + m2 + 1, 256), 256, 0, s>>>(ng, m2, v0, c.g.indices, c.g.adj, ind.get(),
+                                                                       ad.get());
+        CK_LAUNCH("k_local_graph");
+        if (indices) CK(cudaMemcpyAsync(indices, ind.get(), 4 * ((size_t)ng + 1), cudaMemcpyDeviceToHost, s));
+        if (adj && m2) CK(cudaMemcpyAsync(adj, ad.get(), 4 * (size_t)m2, cudaMemcpyDeviceToHost, s));
+        if (tri && ng) CK(cudaMemcpyAsync(tri, c.g.tri + v0, 4 * (size_t)ng, cudaMemcpyDeviceToHost, s));
+        if (tri_deg && ng) CK(cudaMemcpyAsync(tri_deg, c.g.tri_deg + v0, 4 * (size_t)ng, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int scd_batch_run(scd_ctx *ctx, double threshold, int max_iters, scd_result *results) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_graph(c);
+        if (max_iters < 0) throw Error(SCD_ERR_ARG, "max_iters < 0");
+        RunOut o;
+        run_loop(c, threshold, max_iters, nullptr, 0, o);
+        bool all = true;
+        for (uint32_t g = 0; g < c.b.G; g++) {
+            const uint32_t ng = c.b.h_fin_off[g + 1] - c.b.h_fin_off[g];
+            if (results) {
+                scd_result &r = results[g];
+                memset(&r, 0, sizeof r);
+                r.iterations = o.iters[g];
+                r.initial_wcc = o.wcc0[g];
+                r.best_wcc = o.best[g];
+                r.initial_communities = c.b.h_comm_off[g + 1] - c.b.h_comm_off[g];
+                r.distinct_communities = o.distinct[g];
+                r.printed_communities = ng - o.distinct[g];
+                r.ms_partition = o.ms_partition;
+                r.ms_iterations = o.ms_iterations;
+            }
+            if (o.active[g]) all = false;
+        }
+        if (!all) throw Error(SCD_ERR_LIMIT, "some graphs were still improving after max_iters");
+    });
+}
+
+int scd_batch_labels(scd_ctx *ctx, uint32_t g, uint32_t *labels) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_labels(c);
+        if (g >= c.b.G) throw Error(SCD_ERR_ARG, "graph index out of range");
+        cudaStream_t s = c.stream;
+        const uint32_t v0 = c.b.h_fin_off[g], ng = c.b.h_fin_off[g + 1] - v0;
+        if (!ng) return;
+        DevBuf<uint32_t> tmp(ng, s);
+        k_local_labels<<<grid_for(ng, 256), 256, 0, s>>>(ng, v0, c.b.h_comm_off[g], c.best, tmp.get());
+        CK_LAUNCH("k_local_labels");
+        CK(cudaMemcpyAsync(labels, tmp.get(), 4 * (size_t)ng, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
     });
 }
 

@@ -33,8 +33,7 @@ struct Graph {
     uint32_t n = 0, m = 0;
     uint32_t *indices = nullptr, *adj = nullptr, *nlow = nullptr;
     int32_t *tri = nullptr, *tri_deg = nullptr;
-    double p_ext = 0.0;
-    double *p_ext_dev = nullptr;
+    double p_ext = 0.0;   // of graph 0 (the only graph of a plain context)
     uint32_t max_deg = 0;
     // degree buckets of the improve kernels, built once per graph
     DegreeClasses cls;
@@ -44,6 +43,33 @@ struct Graph {
 
 struct Stats {
     int32_t *sizes = nullptr, *ext = nullptr, *intl = nullptr;
+};
+
+// The graphs of a context.  A batch of G independent graphs is held as one
+// block-diagonal union graph: graph g owns the vertex range
+// [fin_off[g], fin_off[g+1]) and the label range [comm_off[g], comm_off[g+1]),
+// so every kernel runs once over all graphs, while everything that is defined
+// per graph (p_ext, the WCC and its summation order, the convergence test) is
+// kept per graph.  A plain context is a batch with G = 1.
+struct Batch {
+    uint32_t G = 1;
+    uint32_t *fin_off = nullptr;          // device, G+1
+    std::vector<uint32_t> h_fin_off;      // host copy
+    std::vector<uint32_t> h_m;            // undirected edges per graph
+    uint32_t *gid = nullptr;              // device, n: graph of each vertex (nullptr if G == 1)
+    double *p_ext = nullptr;              // device, G
+    std::vector<double> h_p_ext;
+    uint32_t *comm_off = nullptr;         // device, G+1 (labels of the initial partition)
+    std::vector<uint32_t> h_comm_off;
+    uint32_t *blk_off = nullptr;          // device, G+1: WCC partial blocks of each graph
+    uint32_t *blk_gid = nullptr;          // device, #blocks: graph of each WCC block
+    uint32_t blocks = 0;
+    double *wcc = nullptr;                // device, G: WCC of the current labels
+    double *best_wcc = nullptr;           // device, G
+    uint8_t *active = nullptr;            // device, G: still iterating
+    uint8_t *improved = nullptr;          // device, G: last iteration beat the best
+    int32_t *iters = nullptr;             // device, G
+    uint32_t *n_active = nullptr;         // device, 1
 };
 
 // CUDA-event phase timers (active with SCD_FLAG_PROFILE)
@@ -84,6 +110,9 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
 // With labels: internal triangles only.  tcount and flag must be zeroed.
 void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, const uint32_t *labels, uint32_t *tcount,
                      uint8_t *flag, cudaStream_t s);
+// set kernel attributes (dynamic shared memory) once per device, outside any capture
+void prepare_tc_kernels();
+void prepare_improve_kernels();
 
 struct Ctx;
 // records [start, end) of a phase on the context's stream when profiling
@@ -106,7 +135,9 @@ struct Ctx {
     uint64_t launches = 0;
 
     Graph g;
+    Batch b;
     bool has_graph = false;
+    bool capturing = false;           // inside a CUDA-graph capture: no host syncs, no timers
 
     // partition state
     uint32_t *labels = nullptr, *labels_next = nullptr, *best = nullptr;
@@ -118,7 +149,8 @@ struct Ctx {
     uint32_t *itcount = nullptr;      // internal triangles per vertex
     int32_t *itdeg = nullptr;         // edges on an internal triangle per vertex
     TcPlan wplan;                     // triangle-counting plan of the resident graph
-    double *wcc_part = nullptr, *wcc_sum = nullptr, *wcc_host = nullptr;
+    double *wcc_part = nullptr, *wcc_host = nullptr;
+    uint32_t *host_u32 = nullptr;     // pinned: the active-graph count of an iteration
     uint32_t *big_tables = nullptr;   // global hash tables of the last degree bucket
     double *pin64 = nullptr;          // per-community p_in of the current statistics
     float2 *pin32 = nullptr;          // and its FP32 enclosure
@@ -141,7 +173,9 @@ struct Ctx {
 };
 
 // preprocess.cu
-void convert_edges(Ctx &c, const uint32_t *pairs_dev, uint64_t count);
+// rec_off (host, G+1 entries, nullable): records of graph g are [rec_off[g], rec_off[g+1]),
+// each graph with its own vertex ids; the graphs become one block-diagonal union.
+void convert_edges(Ctx &c, const uint32_t *pairs_dev, uint64_t count, const std::vector<uint64_t> *rec_off = nullptr);
 void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
                   const int32_t *tri, const int32_t *tri_deg);
 void finish_graph(Ctx &c);   // nlow, p_ext, degree classes, partition buffers
@@ -153,8 +187,13 @@ void initial_partition(Ctx &c);
 // refine.cu
 void collect_stats(Ctx &c, const uint32_t *labels, Stats &st);
 double compute_wcc(Ctx &c, const uint32_t *labels, const Stats &st);
-void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next);
-void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st);   // result in c.wcc_sum (device)
+// frozen_graphs: vertices of graphs whose loop has ended keep their labels
+void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bool frozen_graphs = false);
+void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st);   // per-graph WCC in c.b.wcc (device)
 void compute_p_ext(Ctx &c);
+// per-graph loop control after a WCC (src/main.cpp:68-81): iteration count,
+// best WCC, best labels, convergence; *n_active receives the graphs still running
+void batch_step(Ctx &c, double threshold, double *trace = nullptr, int max_trace = 0);
+void batch_reset(Ctx &c);   // best := current WCC, all non-empty graphs active
 
 }  // namespace scd

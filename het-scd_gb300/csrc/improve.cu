@@ -31,10 +31,14 @@ struct ImproveArgs {
     Stats st;
     const double *pin64;   // p_in of every community (src/scd.cpp:296-298)
     const float2 *pin32;   // its FP32 enclosure
-    const double *p_ext_ptr;
+    const double *p_ext;      // per graph
+    const uint32_t *gid;      // graph of each vertex (nullptr: one graph)
+    const uint8_t *active;    // per graph: still iterating (nullptr: all)
     double alpha;
     uint32_t *next;
 };
+
+__device__ __forceinline__ uint32_t graph_of(const ImproveArgs &a, uint32_t p) { return a.gid ? a.gid[p] : 0u; }
 
 __device__ __forceinline__ bool better(double g1, uint32_t l1, double g2, uint32_t l2) {
     return g1 > g2 || (g1 == g2 && l1 < l2);
@@ -88,8 +92,7 @@ k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs 
     constexpr int PER_WARP = 32 / G;
     const int lane = threadIdx.x & 31, gl = lane % G, g0 = lane - gl;
     const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << g0);
-    const double p_ext = *a.p_ext_ptr;
-    const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
+    const Iv al = iv_of(a.alpha);
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * PER_WARP < count; w += warps) {
         const uint32_t slot = w * PER_WARP + lane / G;
@@ -98,7 +101,11 @@ k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs 
         const uint32_t beg = active ? a.indices[p] : 0;
         const uint32_t deg = active ? a.indices[p + 1] - beg : 0;
         const uint32_t mine = active ? a.labels[p] : INVALID;
-        const uint32_t l = (uint32_t)gl < deg ? a.labels[a.adj[beg + gl]] : INVALID;
+        const uint32_t gp = active ? graph_of(a, p) : 0u;
+        const bool frozen = active && a.active && !a.active[gp];   // graph already converged
+        const double p_ext = a.p_ext[gp];
+        const Iv pe = iv_of(p_ext);
+        const uint32_t l = (uint32_t)gl < deg && !frozen ? a.labels[a.adj[beg + gl]] : INVALID;
         const unsigned peers = __match_any_sync(FULL, l) & gmask;
         const bool owner = l != INVALID && lane == __ffs(peers) - 1;
         const uint32_t freq = __popc(peers);
@@ -135,7 +142,8 @@ k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs 
                 bl = ol;
             }
         }
-        if (active && gl == 0) a.next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, remove_gain, mine);
+        if (active && gl == 0)
+            a.next[p] = frozen ? mine : decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, remove_gain, mine);
     }
 }
 
@@ -260,14 +268,18 @@ __global__ void __launch_bounds__(THREADS)
 k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
     extern __shared__ uint32_t smem[];
     uint32_t *keys = smem, *vals = smem + CAP, *list = smem + 2 * CAP;
-    const double p_ext = *a.p_ext_ptr;
-    const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
+    const Iv al = iv_of(a.alpha);
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
         const uint32_t p = verts[i];
+        const uint32_t gp = graph_of(a, p);
+        if (a.active && !a.active[gp]) {   // graph already converged: labels stay
+            if (threadIdx.x == 0) a.next[p] = a.labels[p];
+            continue;
+        }
         const uint32_t deg = a.indices[p + 1] - a.indices[p];
         uint32_t cap = 64;
         while (cap < 2 * deg) cap <<= 1;
-        improve_cta<THREADS>(a, p, keys, vals, list, cap, p_ext, pe, al);
+        improve_cta<THREADS>(a, p, keys, vals, list, cap, a.p_ext[gp], iv_of(a.p_ext[gp]), al);
     }
 }
 
@@ -277,39 +289,69 @@ constexpr int GLOBAL_THREADS = 512;
 __global__ void __launch_bounds__(GLOBAL_THREADS)
 k_improve_global(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a, uint32_t *tables,
                  const uint64_t *__restrict__ table_off) {
-    const double p_ext = *a.p_ext_ptr;
-    const Iv pe = iv_of(p_ext), al = iv_of(a.alpha);
+    const Iv al = iv_of(a.alpha);
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
+        const uint32_t p = verts[i];
+        const uint32_t gp = graph_of(a, p);
+        if (a.active && !a.active[gp]) {
+            if (threadIdx.x == 0) a.next[p] = a.labels[p];
+            continue;
+        }
         const uint64_t off = table_off[i];
         const uint32_t cap = (uint32_t)((table_off[i + 1] - off) / 3);
         uint32_t *t = tables + off;
-        improve_cta<GLOBAL_THREADS>(a, verts[i], t, t + cap, t + 2 * cap, cap, p_ext, pe, al);
+        improve_cta<GLOBAL_THREADS>(a, p, t, t + cap, t + 2 * cap, cap, a.p_ext[gp], iv_of(a.p_ext[gp]), al);
     }
 }
 
 template <int THREADS, uint32_t CAP>
-void launch_cta(const uint32_t *verts, uint32_t count, const ImproveArgs &a, cudaStream_t s, unsigned max_grid) {
-    const size_t smem = (2 * CAP + CAP / 2) * sizeof(uint32_t);
-    if (smem > 48 * 1024)
+constexpr size_t cta_smem() {
+    return (2 * CAP + CAP / 2) * sizeof(uint32_t);
+}
+
+template <int THREADS, uint32_t CAP>
+void set_cta_attr() {
+    if (cta_smem<THREADS, CAP>() > 48 * 1024)
         CK(cudaFuncSetAttribute((const void *)k_improve_cta<THREADS, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem));
-    k_improve_cta<THREADS, CAP><<<grid_for(count, 1, max_grid), THREADS, smem, s>>>(verts, count, a);
+                                (int)cta_smem<THREADS, CAP>()));
+}
+
+}  // namespace
+
+void prepare_improve_kernels() {
+    static thread_local int done_device = -1;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (done_device == dev) return;
+    set_cta_attr<128, 512>();
+    set_cta_attr<256, 4096>();
+    set_cta_attr<512, 16384>();
+    done_device = dev;
+}
+
+namespace {
+
+template <int THREADS, uint32_t CAP>
+void launch_cta(const uint32_t *verts, uint32_t count, const ImproveArgs &a, cudaStream_t s, unsigned max_grid) {
+    k_improve_cta<THREADS, CAP><<<grid_for(count, 1, max_grid), THREADS, cta_smem<THREADS, CAP>(), s>>>(verts, count, a);
     CK_LAUNCH("k_improve_cta");
 }
 
 }  // namespace
 
-void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next) {
+void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bool frozen_graphs) {
     const Graph &g = c.g;
     cudaStream_t s = c.stream;
     if (g.n == 0) return;
     PhaseScope ph(c, "improve");
+    prepare_improve_kernels();
     if (c.num_comms) {
         k_comm_prep<<<grid_for(c.num_comms, TPB), TPB, 0, s>>>(c.num_comms, st, c.pin64, c.pin32);
         CK_LAUNCH("k_comm_prep");
         c.launches++;
     }
-    ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.pin32, g.p_ext_dev, c.alpha, next};
+    ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.pin32, c.b.p_ext, c.b.gid,
+                  frozen_graphs ? c.b.active : nullptr, c.alpha, next};
     const DegreeClasses &k = g.cls;
     if (k.count[0]) {
         k_improve_group<8><<<grid_for((uint64_t)k.count[0] * 8, TPB), TPB, 0, s>>>(k.list[0], k.count[0], a);

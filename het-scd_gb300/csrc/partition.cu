@@ -41,6 +41,18 @@ __global__ void k_cc_keys(uint32_t n, const uint32_t *__restrict__ order, const 
     }
 }
 
+__global__ void k_graph_keys(uint32_t n, const uint32_t *__restrict__ order, const uint32_t *__restrict__ gid,
+                             uint64_t *keys) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) keys[i] = gid[order[i]];
+}
+
+// label offset of every graph: the seed rank at the graph's first position
+__global__ void k_comm_off(uint32_t G, const uint32_t *__restrict__ fin_off, const uint32_t *__restrict__ rank,
+                           uint32_t *comm_off) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x)
+        comm_off[g] = rank[fin_off[g]];
+}
+
 __global__ void k_positions(uint32_t n, const uint32_t *__restrict__ order, uint32_t *pos) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[order[i]] = i;
 }
@@ -121,6 +133,8 @@ void initial_partition(Ctx &c) {
     const uint32_t n = g.n;
     c.num_comms = 0;
     if (n == 0) {
+        c.b.h_comm_off.assign(c.b.G + 1, 0);
+        CK(cudaMemsetAsync(c.b.comm_off, 0, 4 * (c.b.G + 1), s));
         c.has_labels = true;
         return;
     }
@@ -133,6 +147,12 @@ void initial_partition(Ctx &c) {
     k_cc_keys<<<grid_for(n, TPB), TPB, 0, s>>>(n, order.get(), g.indices, g.tri, keys.get());
     CK_LAUNCH("k_cc_keys");
     radix_sort<uint64_t>(keys.get(), order.get(), n, 0, 64, s);
+    if (c.b.G > 1) {   // graph-major: each graph's order stays contiguous
+        k_graph_keys<<<grid_for(n, TPB), TPB, 0, s>>>(n, order.get(), c.b.gid, keys.get());
+        CK_LAUNCH("k_graph_keys");
+        radix_sort<uint64_t>(keys.get(), order.get(), n, 0, ceil_log2(c.b.G), s);
+        c.launches++;
+    }
     keys.release();
     k_positions<<<grid_for(n, TPB), TPB, 0, s>>>(n, order.get(), pos.get());
     CK_LAUNCH("k_positions");
@@ -160,8 +180,12 @@ void initial_partition(Ctx &c) {
     k_claim_labels<<<G, TPB, 0, s>>>(n, g.indices, g.adj, pos.get(), state.get(), c.labels);
     CK_LAUNCH("k_claim_labels");
     c.launches += 4;
-    CK(cudaMemcpyAsync(&c.num_comms, rank.get() + n, 4, cudaMemcpyDeviceToHost, s));
+    k_comm_off<<<grid_for(c.b.G + 1, TPB), TPB, 0, s>>>(c.b.G, c.b.fin_off, rank.get(), c.b.comm_off);
+    CK_LAUNCH("k_comm_off");
+    c.b.h_comm_off.resize(c.b.G + 1);
+    CK(cudaMemcpyAsync(c.b.h_comm_off.data(), c.b.comm_off, 4 * (c.b.G + 1), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    c.num_comms = c.b.h_comm_off[c.b.G];
     c.cur = 0;
     collect_stats(c, c.labels, c.st[0]);
     CK(cudaMemcpyAsync(c.best, c.labels, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));

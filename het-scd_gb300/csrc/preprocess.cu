@@ -162,13 +162,15 @@ __global__ void k_degree_keys(const int32_t *__restrict__ tri_deg, uint32_t n, i
     }
 }
 
+// final id = number of kept vertices before v in the sorted order
 __global__ void k_rank_of(const uint32_t *__restrict__ order, uint32_t n, const int32_t *__restrict__ tri,
-                          const int32_t *__restrict__ tri_deg, uint32_t *rank, int32_t *tri_out,
-                          int32_t *tri_deg_out, uint32_t n_keep) {
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
-        uint32_t v = order[r];
-        rank[v] = r;
-        if (r < n_keep) {
+                          const int32_t *__restrict__ tri_deg, const uint32_t *__restrict__ kscan, uint32_t *rank,
+                          int32_t *tri_out, int32_t *tri_deg_out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t v = order[i];
+        if (tri_deg[v] > 0) {
+            const uint32_t r = kscan[i];
+            rank[v] = r;
             tri_out[r] = tri[v];
             tri_deg_out[r] = tri_deg[v];
         }
@@ -207,6 +209,74 @@ __global__ void k_split_keys(const uint64_t *__restrict__ keys, uint32_t count, 
     }
 }
 
+// ---- batches: graph g's records are [rec_off[g], rec_off[g+1]) --------------
+
+__device__ __forceinline__ uint32_t segment_of(const uint64_t *off, uint32_t G, uint64_t i) {
+    uint32_t lo = 0, hi = G + 1;   // last g with off[g] <= i
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= i) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo - 1;
+}
+
+__device__ __forceinline__ uint32_t segment_of32(const uint32_t *off, uint32_t G, uint32_t i) {
+    uint32_t lo = 0, hi = G + 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (off[mid] <= i) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo - 1;
+}
+
+// ids of graph g span [0, gmax[g]): one past its largest id
+__global__ void k_graph_id_span(const uint32_t *__restrict__ pairs, uint64_t count, const uint64_t *__restrict__ rec_off,
+                                uint32_t G, uint32_t *gmax) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t g = segment_of(rec_off, G, i);
+        const uint32_t a = pairs[2 * i], b = pairs[2 * i + 1];
+        atomicMax(gmax + g, (a > b ? a : b) + 1);
+    }
+}
+
+// disjoint id ranges: graph g's ids shifted by raw_off[g]
+__global__ void k_offset_pairs(const uint32_t *__restrict__ pairs, uint64_t count, const uint64_t *__restrict__ rec_off,
+                               uint32_t G, const uint64_t *__restrict__ raw_off, uint32_t *out) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t d = (uint32_t)raw_off[segment_of(rec_off, G, i)];
+        out[2 * i] = pairs[2 * i] + d;
+        out[2 * i + 1] = pairs[2 * i + 1] + d;
+    }
+}
+
+// renamed vertices per graph (raw ids of graph g lie in [raw_off[g], raw_off[g+1]))
+__global__ void k_count_renamed(const uint32_t *__restrict__ rename, uint32_t n_raw, const uint64_t *__restrict__ raw_off,
+                                uint32_t G, uint32_t *ndist) {
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n_raw; x += gridDim.x * blockDim.x)
+        if (rename[x] != INVALID) atomicAdd(ndist + segment_of(raw_off, G, x), 1u);
+}
+
+__global__ void k_graph_of_order(const uint32_t *__restrict__ order, uint32_t n, const uint32_t *__restrict__ ren_off,
+                                 uint32_t G, uint64_t *keys) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        keys[i] = segment_of32(ren_off, G, order[i]);
+}
+
+struct KeptAt {
+    const uint32_t *order;
+    const int32_t *tri_deg;
+    __device__ uint32_t operator[](size_t i) const { return tri_deg[order[i]] > 0; }
+};
+
+// first final id of every graph: kept vertices before the graph's first sorted position
+__global__ void k_final_offsets(uint32_t G, const uint32_t *__restrict__ ren_off, const uint32_t *__restrict__ kscan,
+                                uint32_t *fin_off) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x)
+        fin_off[g] = kscan[ren_off[g]];
+}
+
 template <typename T>
 T read_scalar(const T *dev, cudaStream_t s) {
     T h;
@@ -217,16 +287,50 @@ T read_scalar(const T *dev, cudaStream_t s) {
 
 }  // namespace
 
-void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
+void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::vector<uint64_t> *rec_off_h) {
     cudaStream_t s = c.stream;
     if (count >= (1ull << 31)) throw Error(SCD_ERR_LIMIT, "more than 2^31-1 edge records");
+    const uint32_t NG = rec_off_h ? (uint32_t)rec_off_h->size() - 1 : 1;
     c.free_all();
-    if (count == 0) {
+    if (count == 0 && NG == 1) {
         upload_graph(c, 0, 0, nullptr, nullptr, nullptr, nullptr);
         return;
     }
     PhaseScope ph(c, "convert");
-    const unsigned G = grid_for(count, TPB, 152 * 32);
+    const unsigned G = grid_for(count ? count : 1, TPB, 152 * 32);
+    prepare_tc_kernels();
+
+    // 0. a batch: disjoint raw id ranges per graph
+    const uint32_t *pairs = pairs_in;
+    DevBuf<uint64_t> rec_off, raw_off;
+    DevBuf<uint32_t> shifted;
+    if (NG > 1) {
+        rec_off.alloc(NG + 1, s);
+        CK(cudaMemcpyAsync(rec_off.get(), rec_off_h->data(), 8 * (NG + 1), cudaMemcpyHostToDevice, s));
+        DevBuf<uint32_t> gmax(NG, s);
+        CK(cudaMemsetAsync(gmax.get(), 0, 4 * NG, s));
+        if (count) {
+            k_graph_id_span<<<G, TPB, 0, s>>>(pairs_in, count, rec_off.get(), NG, gmax.get());
+            CK_LAUNCH("k_graph_id_span");
+        }
+        raw_off.alloc(NG + 1, s);
+        scan_exclusive<uint64_t>(gmax.get(), raw_off.get(), NG, s);
+        if (read_scalar(raw_off.get() + NG, s) >= 0xffffffffull)
+            throw Error(SCD_ERR_LIMIT, "the graphs of a batch need more than 2^32-1 vertex ids together");
+        shifted.alloc(2 * count + 1, s);
+        if (count) {
+            k_offset_pairs<<<G, TPB, 0, s>>>(pairs_in, count, rec_off.get(), NG, raw_off.get(), shifted.get());
+            CK_LAUNCH("k_offset_pairs");
+        }
+        pairs = shifted.get();
+        c.launches += 3;
+    }
+    if (count == 0) {   // a batch of empty graphs
+        c.b.G = NG;
+        c.b.h_fin_off.assign(NG + 1, 0);
+        upload_graph(c, 0, 0, nullptr, nullptr, nullptr, nullptr);
+        return;
+    }
 
     // 1. first-appearance renumbering
     DevBuf<uint32_t> mx(1, s);
@@ -250,6 +354,18 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
     const uint32_t n1 = read_scalar(wpre.get() + words, s);
     bits.release();
     wpre.release();
+    DevBuf<uint32_t> ren_off(NG + 1, s);   // renamed ids of graph g: [ren_off[g], ren_off[g+1])
+    if (NG > 1) {
+        DevBuf<uint32_t> ndist(NG, s);
+        CK(cudaMemsetAsync(ndist.get(), 0, 4 * NG, s));
+        k_count_renamed<<<grid_for(n_raw, TPB), TPB, 0, s>>>(rename.get(), n_raw, raw_off.get(), NG, ndist.get());
+        CK_LAUNCH("k_count_renamed");
+        scan_exclusive<uint32_t>((const uint32_t *)ndist.get(), ren_off.get(), NG, s);
+        c.launches += 2;
+    } else {
+        const uint32_t h[2] = {0, n1};
+        CK(cudaMemcpyAsync(ren_off.get(), h, 8, cudaMemcpyHostToDevice, s));
+    }
 
     // 2. de-duplicated symmetric CSR over the renamed ids
     const int k1 = ceil_log2(n1 < 2 ? 2 : n1);
@@ -305,20 +421,21 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
     obeg.release();
     olen.release();
 
-    // 4. rank by (tri_deg, id) descending; trim vertices without triangle edges
-    DevBuf<uint32_t> nkeep(2, s);
-    {
-        DevBuf<uint32_t> tmp(n1 + 1, s);
-        scan_exclusive<uint32_t>(NonZeroDeg{tdeg1.get()}, tmp.get(), n1, s);
-        CK(cudaMemcpyAsync(nkeep.get(), tmp.get() + n1, 4, cudaMemcpyDeviceToDevice, s));
-    }
-    const uint32_t n2 = read_scalar(nkeep.get(), s);
+    // 4. rank by (tri_deg, id) descending within each graph; trim vertices
+    //    without triangle edges; final ids count the kept vertices in that order
     DevBuf<uint64_t> dkeys(n1, s);
-    DevBuf<uint32_t> order(n1, s), rank(n1, s);
+    DevBuf<uint32_t> order(n1, s), rank(n1, s), kscan(n1 + 1, s);
     k_degree_keys<<<grid_for(n1, TPB), TPB, 0, s>>>(tdeg1.get(), n1, k1, dkeys.get(), order.get());
     CK_LAUNCH("k_degree_keys");
     radix_sort<uint64_t>(dkeys.get(), order.get(), n1, 0, 32 + k1, s);
+    if (NG > 1) {   // graph-major (stable): each graph's vertices stay contiguous
+        k_graph_of_order<<<grid_for(n1, TPB), TPB, 0, s>>>(order.get(), n1, ren_off.get(), NG, dkeys.get());
+        CK_LAUNCH("k_graph_of_order");
+        radix_sort<uint64_t>(dkeys.get(), order.get(), n1, 0, ceil_log2(NG), s);
+    }
     dkeys.release();
+    scan_exclusive<uint32_t>(KeptAt{order.get(), tdeg1.get()}, kscan.get(), n1, s);
+    const uint32_t n2 = read_scalar(kscan.get() + n1, s);
 
     // 5. final symmetric CSR in rank ids
     DevBuf<uint32_t> fpos(m1 + 1, s);
@@ -332,9 +449,15 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
     g.adj = c.alloc<uint32_t>(2 * (size_t)m2);
     g.tri = c.alloc<int32_t>(n2);
     g.tri_deg = c.alloc<int32_t>(n2);
-    k_rank_of<<<grid_for(n1, TPB), TPB, 0, s>>>(order.get(), n1, tri1.get(), tdeg1.get(), rank.get(), g.tri,
-                                               g.tri_deg, n2);
+    k_rank_of<<<grid_for(n1, TPB), TPB, 0, s>>>(order.get(), n1, tri1.get(), tdeg1.get(), kscan.get(), rank.get(),
+                                               g.tri, g.tri_deg);
     CK_LAUNCH("k_rank_of");
+    c.b.G = NG;
+    c.b.fin_off = c.alloc<uint32_t>(NG + 1);
+    k_final_offsets<<<grid_for(NG + 1, TPB), TPB, 0, s>>>(NG, ren_off.get(), kscan.get(), c.b.fin_off);
+    CK_LAUNCH("k_final_offsets");
+    c.b.h_fin_off.resize(NG + 1);
+    CK(cudaMemcpyAsync(c.b.h_fin_off.data(), c.b.fin_off, 4 * (NG + 1), cudaMemcpyDeviceToHost, s));
     if (m2 > 0) {
         const int k2 = ceil_log2(n2 < 2 ? 2 : n2);
         DevBuf<uint64_t> fkeys(2 * (size_t)m2, s);
@@ -357,7 +480,11 @@ void convert_edges(Ctx &c, const uint32_t *pairs, uint64_t count) {
 void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
                   const int32_t *tri, const int32_t *tri_deg) {
     cudaStream_t s = c.stream;
+    const uint32_t NG = c.b.G;   // > 1 only for a batch of empty graphs
     c.free_all();
+    c.b.G = NG;
+    c.b.h_fin_off.assign(NG + 1, 0);
+    c.b.h_fin_off[NG] = n;
     Graph &g = c.g;
     g.n = n;
     g.m = m;

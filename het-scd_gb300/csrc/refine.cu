@@ -86,27 +86,38 @@ __device__ __forceinline__ double block_sum_fixed(double v, double *sh) {
     return r;
 }
 
+// Graph-aligned blocks: block b sums WCC_CHUNK consecutive vertices of graph
+// blk_gid[b], counted from that graph's first vertex, so every graph's sum has
+// the same shape as when the graph is processed alone.
 __global__ void __launch_bounds__(TPB)
-k_wcc_partial(uint32_t n, const uint32_t *__restrict__ labels, Stats st, const int32_t *__restrict__ tri,
-              const int32_t *__restrict__ tri_deg, const uint32_t *__restrict__ itcount,
-              const int32_t *__restrict__ itdeg, double alpha, double *partial) {
+k_wcc_partial(const uint32_t *__restrict__ fin_off, const uint32_t *__restrict__ blk_off,
+              const uint32_t *__restrict__ blk_gid, const uint32_t *__restrict__ labels, Stats st,
+              const int32_t *__restrict__ tri, const int32_t *__restrict__ tri_deg,
+              const uint32_t *__restrict__ itcount, const int32_t *__restrict__ itdeg, double alpha,
+              double *partial) {
     __shared__ double sh[TPB / 32];
-    const uint32_t base = blockIdx.x * WCC_CHUNK + threadIdx.x * WCC_ITEMS;
+    const uint32_t g = blk_gid[blockIdx.x];
+    const uint32_t end = fin_off[g + 1];
+    const uint32_t base = fin_off[g] + (blockIdx.x - blk_off[g]) * WCC_CHUNK + threadIdx.x * WCC_ITEMS;
     double s = 0.0;
 #pragma unroll
     for (int i = 0; i < WCC_ITEMS; i++)
-        if (base + i < n) s = dadd(s, wcc_term(base + i, labels, st, tri, tri_deg, itcount, itdeg, alpha));
+        if (base + i < end) s = dadd(s, wcc_term(base + i, labels, st, tri, tri_deg, itcount, itdeg, alpha));
     double r = block_sum_fixed(s, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = r;
 }
 
-__global__ void __launch_bounds__(TPB) k_wcc_final(const double *__restrict__ partial, uint32_t parts, uint32_t n,
-                                                   double *out) {
+// one block per graph: fixed-order sum of the graph's partials, divided by its n
+__global__ void __launch_bounds__(TPB) k_wcc_final(const double *__restrict__ partial,
+                                                   const uint32_t *__restrict__ blk_off,
+                                                   const uint32_t *__restrict__ fin_off, double *out) {
     __shared__ double sh[TPB / 32];
+    const uint32_t g = blockIdx.x;
+    const uint32_t p0 = blk_off[g], parts = blk_off[g + 1] - p0, n = fin_off[g + 1] - fin_off[g];
     double s = 0.0;
-    for (uint32_t i = threadIdx.x; i < parts; i += TPB) s = dadd(s, partial[i]);
+    for (uint32_t i = threadIdx.x; i < parts; i += TPB) s = dadd(s, partial[p0 + i]);
     double r = block_sum_fixed(s, sh);
-    if (threadIdx.x == 0) *out = n > 0 ? ddiv(r, (double)n) : 0.0;
+    if (threadIdx.x == 0) out[g] = n > 0 ? ddiv(r, (double)n) : 0.0;
 }
 
 // ---- p_ext ---------------------------------------------------------------------
@@ -135,7 +146,11 @@ constexpr int SEQ_ITEMS = 8;
 constexpr int SEQ_TILE = SEQ_THREADS * SEQ_ITEMS;
 
 __global__ void __launch_bounds__(SEQ_THREADS)
-k_sequential_sum_exact(const double *__restrict__ term, uint32_t n, double divisor, double *out) {
+k_sequential_sum_exact(const double *__restrict__ terms, const uint32_t *__restrict__ seg_off, double *out) {
+    // one block per segment (graph): sum of terms[seg_off[g] .. seg_off[g+1]) / length
+    const double *term = terms + seg_off[blockIdx.x];
+    const uint32_t n = seg_off[blockIdx.x + 1] - seg_off[blockIdx.x];
+    const double divisor = (double)n;
     __shared__ long long warp_tot[SEQ_THREADS / 32];
     __shared__ double s_val;
     __shared__ uint32_t s_pos, s_event;
@@ -237,21 +252,83 @@ k_sequential_sum_exact(const double *__restrict__ term, uint32_t n, double divis
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = ddiv(s_val, divisor);
+    if (threadIdx.x == 0) out[blockIdx.x] = ddiv(s_val, divisor);
 }
 
-__global__ void k_pext_tree(uint32_t n, const double *__restrict__ term, double *partial) {
+__global__ void k_pext_tree(const uint32_t *__restrict__ fin_off, const uint32_t *__restrict__ blk_off,
+                            const uint32_t *__restrict__ blk_gid, const double *__restrict__ term, double *partial) {
     __shared__ double sh[TPB / 32];
-    const uint32_t base = blockIdx.x * WCC_CHUNK + threadIdx.x * WCC_ITEMS;
+    const uint32_t g = blk_gid[blockIdx.x];
+    const uint32_t end = fin_off[g + 1];
+    const uint32_t base = fin_off[g] + (blockIdx.x - blk_off[g]) * WCC_CHUNK + threadIdx.x * WCC_ITEMS;
     double s = 0.0;
 #pragma unroll
     for (int i = 0; i < WCC_ITEMS; i++)
-        if (base + i < n) s = dadd(s, term[base + i]);
+        if (base + i < end) s = dadd(s, term[base + i]);
     double r = block_sum_fixed(s, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = r;
 }
 
+// ---- per-graph loop control ---------------------------------------------------
+
+// src/main.cpp:68-81 for every graph still iterating: count the iteration,
+// remember whether it beat the best WCC, stop when it is below best*(1+threshold)
+__global__ void k_batch_step(uint32_t G, const double *__restrict__ wcc, double *best, uint8_t *active,
+                             uint8_t *improved, int32_t *iters, double threshold, uint32_t *n_active, double *trace,
+                             int max_trace) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x) {
+        improved[g] = 0;
+        if (!active[g]) continue;
+        const double w = wcc[g], b = best[g];
+        const int it = ++iters[g];
+        if (trace && it <= max_trace) trace[(size_t)g * max_trace + it - 1] = w;
+        if (w > b) improved[g] = 1;
+        if (w < dmul(b, dadd(1.0, threshold))) {
+            active[g] = 0;
+        } else {
+            best[g] = w;
+            atomicAdd(n_active, 1u);
+        }
+    }
+}
+
+__global__ void k_copy_improved(uint32_t n, const uint32_t *__restrict__ gid, const uint8_t *__restrict__ improved,
+                                const uint32_t *__restrict__ labels, uint32_t *best) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        if (improved[gid ? gid[v] : 0]) best[v] = labels[v];
+}
+
+__global__ void k_batch_reset(uint32_t G, const uint32_t *__restrict__ fin_off, const double *__restrict__ wcc,
+                              double *best, uint8_t *active, int32_t *iters) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x) {
+        best[g] = wcc[g];
+        active[g] = fin_off[g + 1] > fin_off[g];
+        iters[g] = 0;
+    }
+}
+
 }  // namespace
+
+void batch_step(Ctx &c, double threshold, double *trace, int max_trace) {
+    Batch &b = c.b;
+    cudaStream_t s = c.stream;
+    CK(cudaMemsetAsync(b.n_active, 0, 4, s));
+    k_batch_step<<<grid_for(b.G, TPB), TPB, 0, s>>>(b.G, b.wcc, b.best_wcc, b.active, b.improved, b.iters, threshold,
+                                                     b.n_active, trace, max_trace);
+    CK_LAUNCH("k_batch_step");
+    if (c.g.n) {
+        k_copy_improved<<<grid_for(c.g.n, TPB), TPB, 0, s>>>(c.g.n, b.gid, b.improved, c.labels, c.best);
+        CK_LAUNCH("k_copy_improved");
+    }
+    c.launches += 2;
+}
+
+void batch_reset(Ctx &c) {
+    Batch &b = c.b;
+    k_batch_reset<<<grid_for(b.G, TPB), TPB, 0, c.stream>>>(b.G, b.fin_off, b.wcc, b.best_wcc, b.active, b.iters);
+    CK_LAUNCH("k_batch_reset");
+    c.launches++;
+}
 
 void collect_stats(Ctx &c, const uint32_t *labels, Stats &st) {
     const Graph &g = c.g;
@@ -271,7 +348,7 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
     const Graph &g = c.g;
     cudaStream_t s = c.stream;
     if (g.n == 0) {
-        CK(cudaMemsetAsync(c.wcc_sum, 0, sizeof(double), s));
+        CK(cudaMemsetAsync(c.b.wcc, 0, sizeof(double) * c.b.G, s));
         return;
     }
     PhaseScope ph(c, "wcc");
@@ -283,50 +360,53 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
     k_internal_degrees<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj,
                                                                         c.slot_flag, c.itdeg);
     CK_LAUNCH("k_internal_degrees");
-    const uint32_t parts = (g.n + WCC_CHUNK - 1) / WCC_CHUNK;
-    k_wcc_partial<<<parts, TPB, 0, s>>>(g.n, labels, st, g.tri, g.tri_deg, c.itcount, c.itdeg, c.alpha, c.wcc_part);
-    CK_LAUNCH("k_wcc_partial");
-    k_wcc_final<<<1, TPB, 0, s>>>(c.wcc_part, parts, g.n, c.wcc_sum);
+    const Batch &b = c.b;
+    if (b.blocks) {
+        k_wcc_partial<<<b.blocks, TPB, 0, s>>>(b.fin_off, b.blk_off, b.blk_gid, labels, st, g.tri, g.tri_deg,
+                                               c.itcount, c.itdeg, c.alpha, c.wcc_part);
+        CK_LAUNCH("k_wcc_partial");
+    }
+    k_wcc_final<<<b.G, TPB, 0, s>>>(c.wcc_part, b.blk_off, b.fin_off, b.wcc);
     CK_LAUNCH("k_wcc_final");
     c.launches += 3;
 }
 
 double compute_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
     launch_wcc(c, labels, st);
-    CK(cudaMemcpyAsync(c.wcc_host, c.wcc_sum, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(c.wcc_host, c.b.wcc, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
     return *c.wcc_host;
 }
 
 void compute_p_ext(Ctx &c) {
     Graph &g = c.g;
+    Batch &b = c.b;
     cudaStream_t s = c.stream;
-    if (g.n == 0) {
-        const double nan = 0.0 / 0.0;
-        CK(cudaMemcpyAsync(g.p_ext_dev, &nan, sizeof(double), cudaMemcpyHostToDevice, s));
-        CK(cudaStreamSynchronize(s));
-        g.p_ext = nan;
-        return;
+    DevBuf<double> term(g.n ? g.n : 1, s);
+    if (g.n) {
+        k_pext_terms<<<grid_for(g.n, TPB), TPB, 0, s>>>(g.n, g.indices, g.tri, term.get());
+        CK_LAUNCH("k_pext_terms");
+        c.launches++;
     }
-    DevBuf<double> term(g.n, s);
-    k_pext_terms<<<grid_for(g.n, TPB), TPB, 0, s>>>(g.n, g.indices, g.tri, term.get());
-    CK_LAUNCH("k_pext_terms");
-    if (c.flags & SCD_FLAG_PEXT_TREE) {
-        const uint32_t parts = (g.n + WCC_CHUNK - 1) / WCC_CHUNK;
-        DevBuf<double> part(parts, s);
-        k_pext_tree<<<parts, TPB, 0, s>>>(g.n, term.get(), part.get());
-        CK_LAUNCH("k_pext_tree");
-        k_wcc_final<<<1, TPB, 0, s>>>(part.get(), parts, g.n, g.p_ext_dev);
+    if ((c.flags & SCD_FLAG_PEXT_TREE) && g.n) {
+        DevBuf<double> part(b.blocks ? b.blocks : 1, s);
+        if (b.blocks) {
+            k_pext_tree<<<b.blocks, TPB, 0, s>>>(b.fin_off, b.blk_off, b.blk_gid, term.get(), part.get());
+            CK_LAUNCH("k_pext_tree");
+        }
+        k_wcc_final<<<b.G, TPB, 0, s>>>(part.get(), b.blk_off, b.fin_off, b.p_ext);
         CK_LAUNCH("k_wcc_final");
         c.launches += 2;
+        // (an empty graph's p_ext is 0 here, NaN in the index-ordered mode like the reference's 0/0)
     } else {
-        k_sequential_sum_exact<<<1, SEQ_THREADS, 0, s>>>(term.get(), g.n, (double)g.n, g.p_ext_dev);
+        k_sequential_sum_exact<<<b.G, SEQ_THREADS, 0, s>>>(term.get(), b.fin_off, b.p_ext);
         CK_LAUNCH("k_sequential_sum_exact");
-        c.launches += 1;
+        c.launches++;
     }
-    c.launches += 1;
-    CK(cudaMemcpyAsync(&g.p_ext, g.p_ext_dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    b.h_p_ext.resize(b.G);
+    CK(cudaMemcpyAsync(b.h_p_ext.data(), b.p_ext, sizeof(double) * b.G, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    g.p_ext = b.h_p_ext[0];
 }
 
 }  // namespace scd

@@ -315,13 +315,22 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
     }
 }
 
+template <int TCAP, int LCAP, int FBITS>
+constexpr size_t tc_cta_smem() {
+    return (size_t)TCAP * 4 + (size_t)LCAP * 4 + ((size_t)1 << FBITS) / 8 + (size_t)TCAP * 2;
+}
+
+template <int THREADS, int TCAP, int LCAP, int FBITS>
+void set_tc_attr() {
+    if (tc_cta_smem<TCAP, LCAP, FBITS>() > 48 * 1024)
+        CK(cudaFuncSetAttribute((const void *)k_tc_cta<THREADS, TCAP, LCAP, FBITS>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_cta_smem<TCAP, LCAP, FBITS>()));
+}
+
 template <int THREADS, int TCAP, int LCAP, int FBITS>
 void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, const uint32_t *labels, uint32_t *tcount,
                    uint8_t *flag, uint32_t *ctr, unsigned grid, cudaStream_t s) {
-    const size_t smem = (size_t)TCAP * 4 + (size_t)LCAP * 4 + ((size_t)1 << FBITS) / 8 + (size_t)TCAP * 2;
-    if (smem > 48 * 1024)
-        CK(cudaFuncSetAttribute((const void *)k_tc_cta<THREADS, TCAP, LCAP, FBITS>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = tc_cta_smem<TCAP, LCAP, FBITS>();
     k_tc_cta<THREADS, TCAP, LCAP, FBITS><<<grid, THREADS, smem, s>>>(o, plan.verts[k], plan.unit_off[k], plan.nverts[k],
                                                             labels, tcount, flag, ctr);
     CK_LAUNCH("k_tc_cta");
@@ -399,10 +408,21 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
     }
 }
 
+void prepare_tc_kernels() {
+    static thread_local int done_device = -1;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (done_device == dev) return;
+    set_tc_attr<128, 2048, 1024, 14>();
+    set_tc_attr<256, 16384, 8192, 17>();
+    done_device = dev;
+}
+
 void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, const uint32_t *labels, uint32_t *tcount,
                      uint8_t *flag, cudaStream_t s) {
     if (o.n == 0) return;
     PhaseScope ph(c, labels ? "wcc_tc" : "tc");
+    prepare_tc_kernels();
     uint32_t *ctr = c.work_counter;
     CK(cudaMemsetAsync(ctr, 0, 16, s));
     if (plan.nverts[0]) {

@@ -71,6 +71,12 @@ def lib():
             "scd_profile_get": ([P, ctypes.c_char_p, ctypes.POINTER(dbl), ctypes.POINTER(u64)], i32),
             "scd_profile_reset": ([P], i32),
             "scd_wcc_static": ([P, P, P, P, P, P, u32, dbl, P, P], i32),
+            "scd_batch_convert": ([P, P, P, u32, i32], i32),
+            "scd_batch_size": ([P, ctypes.POINTER(u32)], i32),
+            "scd_batch_graph_info": ([P, u32, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(dbl)], i32),
+            "scd_batch_graph_download": ([P, u32, P, P, P, P], i32),
+            "scd_batch_run": ([P, dbl, i32, P], i32),
+            "scd_batch_labels": ([P, u32, P], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -209,6 +215,53 @@ class Engine:
         b = ctypes.c_uint64()
         self._check(lib().scd_memory_usage(self._ctx, ctypes.byref(b)))
         return b.value
+
+    # --- batches -------------------------------------------------------------
+    def batch_convert(self, graphs):
+        """Device preprocessing of a list of edge lists ((E_g, 2) uint32 each)."""
+        arrs = [np.ascontiguousarray(p, dtype=np.uint32).reshape(-1, 2) for p in graphs]
+        off = np.zeros(len(arrs) + 1, np.uint64)
+        off[1:] = np.cumsum([a.shape[0] for a in arrs])
+        pairs = np.concatenate(arrs) if arrs else np.zeros((0, 2), np.uint32)
+        self._check(lib().scd_batch_convert(self._ctx, _p(pairs), _p(off), len(arrs), 0))
+
+    def batch_convert_device(self, dev_ptr, record_offsets):
+        off = np.ascontiguousarray(record_offsets, dtype=np.uint64)
+        self._check(lib().scd_batch_convert(self._ctx, dev_ptr, _p(off), len(off) - 1, 1))
+
+    def batch_size(self):
+        g = ctypes.c_uint32()
+        self._check(lib().scd_batch_size(self._ctx, ctypes.byref(g)))
+        return g.value
+
+    def batch_graph_info(self, g):
+        n, m, cc = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
+        self._check(lib().scd_batch_graph_info(self._ctx, g, ctypes.byref(n), ctypes.byref(m), ctypes.byref(cc)))
+        return n.value, m.value, cc.value
+
+    def batch_graph_bytes(self, g):
+        n, m, _ = self.batch_graph_info(g)
+        ind = np.empty(n + 1, np.uint32)
+        adj = np.empty(max(2 * m, 1), np.uint32)
+        tri = np.empty(max(n, 1), np.int32)
+        tdg = np.empty(max(n, 1), np.int32)
+        self._check(lib().scd_batch_graph_download(self._ctx, g, _p(ind), _p(adj), _p(tri), _p(tdg)))
+        hdr = np.array([n, m], np.uint32)
+        return b"".join(a.tobytes() for a in (hdr, ind, adj[: 2 * m], tri[:n], tdg[:n]))
+
+    def batch_run(self, threshold=0.01, max_iters=1000):
+        G = self.batch_size()
+        res = (Result * G)()
+        rc = lib().scd_batch_run(self._ctx, threshold, max_iters, res)
+        if rc not in (OK, -7):
+            self._check(rc)
+        return [r.as_dict() for r in res], rc
+
+    def batch_labels(self, g):
+        n = self.batch_graph_info(g)[0]
+        out = np.empty(max(n, 1), np.uint32)
+        self._check(lib().scd_batch_labels(self._ctx, g, _p(out)))
+        return out[:n]
 
     def stream(self):
         p = ctypes.c_void_p()

@@ -142,6 +142,36 @@ int scd_stream(scd_ctx *ctx, void **stream);
 int scd_profile_get(scd_ctx *ctx, const char *phase, double *total_ms, uint64_t *count);
 int scd_profile_reset(scd_ctx *ctx);
 
+/* ---- Batched SCD ---------------------------------------------------------
+ * Many independent graphs in one context.  They are processed together as one
+ * block-diagonal union graph: every preprocessing, partition and refinement
+ * stage is one launch over all graphs (work units drawn from all of them), and
+ * each refinement iteration is one CUDA-graph replay for all graphs still
+ * running.  Per graph, the arithmetic and the results are identical to
+ * processing that graph alone (convert output, p_ext, labels of every
+ * iteration, WCC bit for bit, iteration count). */
+
+/* Preprocessing (as scd_convert_edges) of num_graphs graphs: the records of
+ * graph g are pairs[2*record_offsets[g] .. 2*record_offsets[g+1]), each graph
+ * numbered in its own id space.  record_offsets is a host array of
+ * num_graphs+1 entries; pairs is a device pointer if pairs_on_device != 0.
+ * Limits: fewer than 2^31 records and 2^32-1 distinct ids in total. */
+int scd_batch_convert(scd_ctx *ctx, const uint32_t *pairs, const uint64_t *record_offsets,
+                      uint32_t num_graphs, int pairs_on_device);
+int scd_batch_size(scd_ctx *ctx, uint32_t *num_graphs);
+/* Sizes and p_ext of graph g of the batch. */
+int scd_batch_graph_info(scd_ctx *ctx, uint32_t g, uint32_t *n, uint32_t *m, double *clustering_coef);
+/* Graph g in the binary-format layout with its own ids (what `convert` writes
+ * for that graph alone); any pointer may be NULL. */
+int scd_batch_graph_download(scd_ctx *ctx, uint32_t g, uint32_t *indices, uint32_t *adj, int32_t *tri,
+                             int32_t *tri_deg);
+/* The refinement loop of every graph (as scd_run); results holds num_graphs
+ * entries.  Returns SCD_ERR_LIMIT if some graph was still improving after
+ * max_iters (its results are those of the last iteration). */
+int scd_batch_run(scd_ctx *ctx, double threshold, int max_iters, scd_result *results);
+/* Best labels of graph g (n_g entries) in that graph's own label numbering. */
+int scd_batch_labels(scd_ctx *ctx, uint32_t g, uint32_t *labels);
+
 /* WCC of a labelling without any device allocation.  It has no counterpart in
  * the reference: it exists for callers that cannot let a library call
  * cudaMalloc/cudaFree — a serving process whose memory pool already holds the
