@@ -135,6 +135,186 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def c4_specs(k):
+    """Batched workload: planted-partition graphs, n log-uniform in [1000, 200000],
+    mean degree D uniform in [8, 40], mixing mu uniform in [0.05, 0.4], internal
+    degree D*(1-mu), community sizes 20..100 (P(s) ~ 1/s), graph i seeded 4+i."""
+    import numpy as np
+    out = []
+    for i in range(k):
+        rng = np.random.default_rng(4 + i)
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(200000))))
+        d = float(rng.uniform(8, 40))
+        mu = float(rng.uniform(0.05, 0.4))
+        out.append((n, d * (1 - mu), mu, 4 + i))
+    return out
+
+
+def _gen_planted(spec):
+    import scdgen
+    n, k_in, mu, seed = spec
+    return scdgen.planted(n, k_in, mu, 20, 100, seed=seed)
+
+
+def generate(fn, specs, threads=8):
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(threads) as ex:
+        return list(ex.map(fn, specs))
+
+
+def split_batches(sizes, cap):
+    """Consecutive runs of graphs with at most `cap` edge records each."""
+    out, cur, tot = [], [], 0
+    for i, e in enumerate(sizes):
+        if cur and tot + e > cap:
+            out.append(cur)
+            cur, tot = [], 0
+        cur.append(i)
+        tot += e
+    if cur:
+        out.append(cur)
+    return out
+
+
+def bench_batched(S, device, args):
+    """4096 planted graphs: block-diagonal batches (each batch one union graph whose
+    kernels run every graph's work together, iterations replayed from CUDA graphs)
+    against a per-graph loop of the plain engine, both through the public API from
+    host edge lists to host labels.  The loop is timed on an evenly spaced sample
+    of the same graphs (the graphs are i.i.d.), and its results are compared with
+    the batched ones for that sample."""
+    import numpy as np
+    import torch
+    k = args.batch_graphs
+    t0 = time.time()
+    graphs = generate(_gen_planted, c4_specs(k))
+    gen_s = time.time() - t0
+    sizes = [g.shape[0] for g in graphs]
+    records = int(sum(sizes))
+    groups = split_batches(sizes, args.batch_records)
+    eng = S.Engine(device)
+    eng.batch_convert([graphs[i] for i in groups[0]])
+    tune = eng.autotune()
+
+    def run_group(ids):
+        eng.batch_convert([graphs[i] for i in ids])
+        res, rc = eng.batch_run(0.01, 1000)
+        labs = [eng.batch_labels(g) for g in range(len(ids))]
+        return res, rc, labs
+
+    run_group(groups[0])                    # warm-up (allocator, module load)
+    torch.cuda.synchronize()
+    launches0 = eng.kernel_launches()
+    t = time.perf_counter()
+    results, not_converged = {}, 0
+    for ids in groups:
+        res, rc, labs = run_group(ids)
+        not_converged += rc != 0
+        for j, i in enumerate(ids):
+            results[i] = (res[j]["iterations"], res[j]["best_wcc"], labs[j])
+    torch.cuda.synchronize()
+    batch_s = time.perf_counter() - t
+    launches = eng.kernel_launches() - launches0
+    mem = eng.memory_usage()
+    eng.close()
+
+    step = max(1, k // args.loop_sample)
+    sample = list(range(0, k, step))[: args.loop_sample]
+    plain = S.Engine(device)
+    plain.convert_edges(graphs[sample[0]])
+    plain.run(0.01, 1000)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    same = True
+    loop_records = 0
+    for i in sample:
+        plain.convert_edges(graphs[i])
+        r = plain.run(0.01, 1000)
+        lab = plain.labels_from_device()
+        loop_records += sizes[i]
+        it, w, bl = results[i]
+        same &= r["iterations"] == it and r["best_wcc"] == w and np.array_equal(lab, bl)
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t
+    plain.close()
+    b_gps = k / batch_s
+    l_gps = len(sample) / loop_s
+    return {"workload": f"{k} planted-partition graphs, n log-uniform [1000,200000], mean degree U[8,40], "
+                        "mu U[0.05,0.4], seeds 4..",
+            "graphs": k, "edges_in": records, "batches": len(groups), "max_records_per_batch": args.batch_records,
+            "graphs_per_s": b_gps, "edges_per_s": records / batch_s, "seconds": batch_s,
+            "gpu_launches": launches, "peak_engine_bytes": mem, "not_converged_batches": not_converged,
+            "per_graph_loop": {"graphs_per_s": l_gps, "edges_per_s": loop_records / loop_s, "sample_graphs": len(sample),
+                               "seconds": loop_s},
+            "speedup_vs_loop": b_gps / l_gps, "identical_on_sample": bool(same),
+            "autotune": {"small_max": tune["small_max"], "warp_max": tune["warp_max"], "cta_max": tune["cta_max"]},
+            "timing": "host wall clock, host edge lists in, host labels out", "generate_s": round(gen_s, 1)}
+
+
+def c5_specs(count, seed=5):
+    """Served workload: 80% planted partition, n log-uniform in [1000, 50000],
+    mean degree 16 (internal 14.4), mu 0.1; 20% R-MAT scale 19..21, edge factor 16."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        if rng.uniform() < 0.8:
+            out.append(("planted", int(np.exp(rng.uniform(np.log(1000), np.log(50000)))), 1000 + i))
+        else:
+            out.append(("rmat", int(rng.integers(19, 22)), 5000 + i))
+    return out
+
+
+def _gen_request(spec):
+    import scdgen
+    kind, size, seed = spec
+    if kind == "planted":
+        return scdgen.planted(size, 14.4, 0.1, 20, 100, seed=seed)
+    return scdgen.rmat(size, 16, 0.57, 0.19, 0.19, seed=seed)
+
+
+def bench_served(S, device, args):
+    """Open-loop Poisson arrivals at a fixed offered rate into the continuous-batching
+    server (120 GB admission budget); latency = submission to labels on the host."""
+    import numpy as np
+    import serve
+    specs = c5_specs(args.serve_requests)
+    t0 = time.time()
+    reqs = generate(_gen_request, specs)
+    gen_s = time.time() - t0
+    rng = np.random.default_rng(55)
+    gaps = rng.exponential(1.0 / args.serve_rate, size=len(reqs))
+    # warm-up: every worker engine runs one small batch
+    srv = serve.Server(device, workers=args.serve_workers, budget_bytes=120e9, max_batch=64)
+    for r in [srv.submit(reqs[i]) for i in range(min(8, len(reqs)))]:
+        r.wait(600)
+    srv.batches.clear()
+    handles = []
+    t = time.perf_counter()
+    nxt = t
+    for i, pairs in enumerate(reqs):
+        nxt += gaps[i]
+        d = nxt - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        handles.append(srv.submit(pairs))
+    for h in handles:
+        h.wait(1200)
+    end = max(h.finished for h in handles)
+    srv.close()
+    lat = [h.latency * 1e3 for h in handles]
+    span = end - t
+    sizes = [b[0] for b in srv.batches]
+    return {"workload": "Poisson arrivals; 80% planted n log-uniform [1000,50000] degree 16 mu 0.1, "
+                        "20% R-MAT scale 19-21 edge factor 16",
+            "requests": len(reqs), "offered_per_s": args.serve_rate, "graphs_per_s": len(reqs) / span,
+            "edges_per_s": sum(p.shape[0] for p in reqs) / span,
+            "p50_ms": serve.percentile(lat, 50), "p99_ms": serve.percentile(lat, 99), "max_ms": max(lat),
+            "workers": args.serve_workers, "budget_gb": 120, "peak_admitted_gb": srv.peak_in_use / 1e9,
+            "batches": len(sizes), "mean_batch": float(np.mean(sizes)) if sizes else 0.0,
+            "generate_s": round(gen_s, 1)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -143,6 +323,14 @@ def main():
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--batch-graphs", type=int, default=4096)
+    ap.add_argument("--batch-records", type=int, default=1 << 28)
+    ap.add_argument("--loop-sample", type=int, default=256)
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-rate", type=float, default=40.0)
+    ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -169,6 +357,8 @@ def main():
     dev_pairs = torch.from_numpy(pairs.view(np.int32)).cuda()
     host_pairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
 
+    # timed engine: CUDA events around the preprocessing phases (the triangle-counting
+    # phase gives the roofline), iterations replayed from captured CUDA graphs
     eng = S.Engine(local, flags=S.FLAG_PROFILE)
     stream = torch.cuda.ExternalStream(eng.stream())
 
@@ -203,7 +393,7 @@ def main():
         dist.barrier()
     dev_ms = ev0.elapsed_time(ev1) / args.steps
     launches = eng.kernel_launches() - launches0
-    prof = {p: eng.profile(p) for p in S.PHASES}
+    tc_ms, tc_n = eng.profile("tc")
     ck = clocks.stop()
     # e2e through the public API with host buffers
     for _ in range(1):
@@ -227,8 +417,18 @@ def main():
     # roofline of the dominant kernel: preprocessing triangle counting
     gd = eng.graph_download()
     b_tc, tcinfo = algorithmic_tc_bytes(gd["indices"], gd["adj"])
-    tc_ms, tc_n = prof["tc"]
     tc_avg = tc_ms / max(tc_n, 1)
+    # phase breakdown: a separate engine launching the iterations kernel by kernel
+    peng = S.Engine(local, flags=S.FLAG_PROFILE | S.FLAG_NO_GRAPHS)
+    for i in range(2):
+        if i == 1:
+            torch.cuda.synchronize()
+            peng.profile_reset()
+        peng.convert_edges(device_ptr=dev_pairs.data_ptr(), count=E)
+        peng.run(0.01, 1000)
+    torch.cuda.synchronize()
+    prof = {p: peng.profile(p) for p in S.PHASES}
+    peng.close()
     peak, peak_kind = measured_peak_gbs()
     achieved = b_tc / (tc_avg / 1e3) / 1e9
 
@@ -241,8 +441,8 @@ def main():
             "e2e": {"value": world * E / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": E * 8,
                     "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1)},
             "gpu_launches": launches,
-            "phases_ms": {p: round(v[0] / max(args.steps, 1), 3) for p, v in prof.items()},
-            "roofline": {"kernel": "k_tc_units (preprocessing triangle counting)", "bound": "hbm",
+            "phases_ms": {p: round(v[0], 3) for p, v in prof.items()},
+            "roofline": {"kernel": "k_tc_warp + k_tc_cta (preprocessing triangle counting)", "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "algorithmic_bytes": b_tc, "ms_per_launch": tc_avg,
                          "traffic": None},
@@ -253,9 +453,14 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": oracle.threads(), "kind": kind,
                                 "sample": f"R-MAT scale {CPU_SAMPLE_SCALE} ({e} edges), same generator; "
                                           f"{t_ms:.0f} ms of reference-timer CPU work"}
+    eng.close()
+    del dev_pairs, host_pairs
+    if not args.no_batched:
+        line["batched"] = bench_batched(S, local, args)
+    if not args.no_served:
+        line["served"] = bench_served(S, local, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
     if dist:
         dist.destroy_process_group()
 

@@ -393,8 +393,9 @@ void iterate_async(Ctx &c, double threshold, double *trace, int max_trace) {
     c.labels = c.labels_next;
     c.labels_next = t;
     c.cur ^= 1;
-    collect_stats(c, c.labels, c.st[c.cur]);
-    launch_wcc(c, c.labels, c.st[c.cur]);
+    // converged graphs of a batch keep their labels; their statistics and WCC are not needed any more
+    collect_stats(c, c.labels, c.st[c.cur], c.b.G > 1);
+    launch_wcc(c, c.labels, c.st[c.cur], c.b.G > 1);
     batch_step(c, threshold, trace, max_trace);
 }
 
@@ -428,6 +429,21 @@ std::vector<uint32_t> distinct_per_graph(Ctx &c, const uint32_t *labels) {
 // The loop of src/main-gpu.cpp:54-95 for every graph of the context at once;
 // each iteration is replayed from a captured CUDA graph (two graphs, one per
 // parity of the label double buffer), with one host read per iteration.
+// Kernel nodes of a captured graph (the launches one replay makes).
+static uint64_t kernel_nodes(cudaGraph_t gr) {
+    size_t n = 0;
+    CK(cudaGraphGetNodes(gr, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) CK(cudaGraphGetNodes(gr, nodes.data(), &n));
+    uint64_t k = 0;
+    for (size_t i = 0; i < n; i++) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nodes[i], &t));
+        k += t == cudaGraphNodeTypeKernel;
+    }
+    return k;
+}
+
 void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int max_trace, RunOut &out) {
     Batch &b = c.b;
     cudaStream_t s = c.stream;
@@ -439,8 +455,9 @@ void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int ma
     CK(cudaMemcpyAsync(out.wcc0.data(), b.wcc, 8 * b.G, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     const double t1 = now_ms();
-    const bool graphs = !(c.flags & SCD_FLAG_PROFILE) && c.g.n > 0;
+    const bool graphs = !(c.flags & SCD_FLAG_NO_GRAPHS) && c.g.n > 0;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    uint64_t kernels[2] = {0, 0};
     try {
         for (int it = 0; it < max_iters; it++) {
             if (graphs) {
@@ -459,6 +476,7 @@ void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int ma
                     }
                     c.capturing = false;
                     CK(cudaStreamEndCapture(s, &gr));
+                    kernels[par] = kernel_nodes(gr);
                     const cudaError_t e = cudaGraphInstantiate(&exec[par], gr, 0);
                     cudaGraphDestroy(gr);
                     CK(e);
@@ -470,7 +488,7 @@ void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int ma
                     c.cur ^= 1;
                 }
                 CK(cudaGraphLaunch(exec[par], s));
-                c.launches += 12;
+                c.launches += kernels[par];
             } else {
                 iterate_async(c, threshold, trace_dev, max_trace);
             }
@@ -669,6 +687,7 @@ int scd_current_labels(scd_ctx *ctx, uint32_t *labels) {
 int scd_community_stats(scd_ctx *ctx, int32_t *sizes, int32_t *ext, int32_t *intl, uint32_t *nc) {
     return guarded(ctx, [&](Ctx &c) {
         require_labels(c);
+        if (c.b.G != 1) throw Error(SCD_ERR_STATE, "the context holds a batch: statistics are per single graph");
         const Stats &st = c.st[c.cur];
         const size_t b = (size_t)c.num_comms * 4;
         if (sizes && b) CK(cudaMemcpyAsync(sizes, st.sizes, b, cudaMemcpyDeviceToHost, c.stream));
@@ -804,6 +823,29 @@ int scd_batch_labels(scd_ctx *ctx, uint32_t g, uint32_t *labels) {
         CK_LAUNCH("k_local_labels");
         CK(cudaMemcpyAsync(labels, tmp.get(), 4 * (size_t)ng, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
+    });
+}
+
+int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t *cta_max, double *best_ms,
+                 char *report, uint64_t report_cap) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_graph(c);
+        std::vector<std::string> lines;
+        const double ms = autotune_tc(c, &lines);
+        if (c.g.n) {   // the WCC plan follows the chosen split
+            c.wplan = TcPlan();
+            tc_plan(c, Oriented{c.g.indices, c.g.nlow, c.g.adj, c.g.n}, c.wplan, c.stream, true);
+        }
+        if (small_max) *small_max = c.tc_small;
+        if (warp_max) *warp_max = c.tc_b0;
+        if (cta_max) *cta_max = c.tc_b1;
+        if (best_ms) *best_ms = ms;
+        if (report && report_cap) {
+            std::string all;
+            for (auto &l : lines) all += l + "\n";
+            strncpy(report, all.c_str(), report_cap - 1);
+            report[report_cap - 1] = 0;
+        }
     });
 }
 

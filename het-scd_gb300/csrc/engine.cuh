@@ -96,9 +96,18 @@ struct Oriented {
     const uint32_t *adj;
     uint32_t n;
 };
+// Label mode of triangle counting: only triangles whose three vertices carry
+// the same valid label count; with `active`, vertices of graphs of a batch that
+// stopped iterating are skipped (their WCC is no longer read).
+struct LabelFilter {
+    const uint32_t *labels = nullptr;   // nullptr: count every triangle
+    const uint32_t *gid = nullptr;
+    const uint8_t *active = nullptr;
+    __device__ __forceinline__ bool frozen(uint32_t v) const { return active && !active[gid[v]]; }
+};
 // out-degree buckets and their work-unit offsets (built once per oriented graph)
 struct TcPlan {
-    static constexpr int K = 4;
+    static constexpr int K = 6;
     uint32_t *verts[K] = {};
     uint32_t *unit_off[K] = {};
     uint32_t nverts[K] = {};
@@ -108,8 +117,10 @@ struct Ctx;
 void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned);
 // tcount[v] += triangles at v; flag[slot] = 1 for out-slots on a triangle.
 // With labels: internal triangles only.  tcount and flag must be zeroed.
-void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, const uint32_t *labels, uint32_t *tcount,
+void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter labels, uint32_t *tcount,
                      uint8_t *flag, cudaStream_t s);
+// times the triangle-counting bucket splits on the resident graph, keeps the fastest
+double autotune_tc(Ctx &c, std::vector<std::string> *report);
 // set kernel attributes (dynamic shared memory) once per device, outside any capture
 void prepare_tc_kernels();
 void prepare_improve_kernels();
@@ -133,6 +144,7 @@ struct Ctx {
     cudaStream_t side = nullptr;
     std::string err;
     uint64_t launches = 0;
+    uint32_t tc_small = 32, tc_b0 = 64, tc_b1 = 1024;   // triangle-counting bucket splits (autotuned)
 
     Graph g;
     Batch b;
@@ -185,11 +197,12 @@ void finish_graph(Ctx &c);   // nlow, p_ext, degree classes, partition buffers
 void initial_partition(Ctx &c);
 
 // refine.cu
-void collect_stats(Ctx &c, const uint32_t *labels, Stats &st);
+void collect_stats(Ctx &c, const uint32_t *labels, Stats &st, bool frozen_graphs = false);
 double compute_wcc(Ctx &c, const uint32_t *labels, const Stats &st);
 // frozen_graphs: vertices of graphs whose loop has ended keep their labels
 void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bool frozen_graphs = false);
-void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st);   // per-graph WCC in c.b.wcc (device)
+// per-graph WCC in c.b.wcc (device); frozen_graphs: skip the graphs of a batch that stopped iterating
+void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_graphs = false);
 void compute_p_ext(Ctx &c);
 // per-graph loop control after a WCC (src/main.cpp:68-81): iteration count,
 // best WCC, best labels, convergence; *n_active receives the graphs still running

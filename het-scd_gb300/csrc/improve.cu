@@ -68,6 +68,31 @@ __device__ __forceinline__ Iv interval_gain(const ImproveArgs &a, uint32_t l, ui
                        exact_needed);
 }
 
+// Interval of the gain of label l, own label included (the negated remove gain:
+// the community without p, as exact_gain's l == mine branch, with
+// community_p_in enclosed).  One wcc_gain_iv call for both kinds, so lanes of a
+// warp holding own and foreign labels do not diverge through it.
+__device__ __forceinline__ Iv interval_any_gain(const ImproveArgs &a, uint32_t l, bool own, uint32_t freq,
+                                                uint32_t deg, Iv p_ext, Iv alpha, bool *exact_needed) {
+    int size = a.st.sizes[l], ext = a.st.ext[l];
+    Iv pin;
+    if (own) {
+        size--;
+        ext += (int)(freq - (deg - freq));
+        const int in = a.st.intl[l] / 2 - (int)freq;
+        pin = size > 1 ? iv_div(iv_int(2 * in), iv_mul(iv_int(size), iv_int(size - 1))) : Iv{0.f, 0.f};
+    } else {
+        const float2 p = a.pin32[l];
+        pin = Iv{p.x, p.y};
+    }
+    return wcc_gain_iv(size, (int)freq, (int)deg - (int)freq, ext, pin, p_ext, alpha, exact_needed);
+}
+
+// The own label's exact gain is needed unless no foreign label survives the
+// interval test and the interval alone fixes the sign of the remove gain
+// (remove gain > 0 exactly when the own gain is < 0).
+__device__ __forceinline__ bool own_sign_known(Iv iv, bool need) { return !need && (iv.hi < 0.f || iv.lo >= 0.f); }
+
 __device__ __forceinline__ uint32_t decide(double best_gain, uint32_t best_label, double remove_gain,
                                            uint32_t mine) {
     const double insert = dadd(best_gain, remove_gain);
@@ -85,16 +110,69 @@ __global__ void k_comm_prep(uint32_t nc, Stats st, double *pin64, float2 *pin32)
 }
 
 // ---- degree <= G: groups of G lanes ---------------------------------------
+//
+// FP64 runs at 1/64 of the FP32 rate on this part and a warp pays for an FP64
+// instruction whatever its active lanes, so the exact gains are not evaluated
+// where they arise (one or two lanes of a group) but queued per warp: each round
+// (32/G vertices) adds at most one item per lane (the own label if its exact
+// gain is needed, every foreign survivor), and once more than QCAP-32 items wait
+// the warp evaluates them with all lanes busy, then decides every pending
+// vertex.  A vertex without items is decided at once from the intervals.
+
+constexpr int QCAP = 64;
+constexpr unsigned GROUP_GRID = 152 * 4;   // resident CTAs (64 registers x 256 threads): warps loop over many rounds
+
+struct GroupQueue {
+    uint32_t label[QCAP], freq[QCAP];
+    double gain[QCAP];
+    uint8_t vert[QCAP];
+    uint32_t p[QCAP], deg[QCAP], mine[QCAP], gp[QCAP];
+    uint8_t first[QCAP], cnt[QCAP];
+};
+
+__device__ __forceinline__ void flush_queue(const ImproveArgs &a, GroupQueue &q, uint32_t qn, uint32_t pend,
+                                            int lane) {
+    __syncwarp();
+    for (uint32_t i = lane; i < qn; i += 32) {
+        const uint32_t v = q.vert[i];
+        q.gain[i] = exact_gain(a, q.label[i], q.freq[i], q.deg[v], q.mine[v], a.p_ext[q.gp[v]]);
+    }
+    __syncwarp();
+    for (uint32_t v = lane; v < pend; v += 32) {
+        const uint32_t mine = q.mine[v], f = q.first[v], e = f + q.cnt[v];
+        double rg = 0.0, bg = 0.0;
+        uint32_t bl = INVALID;
+        for (uint32_t k = f; k < e; k++) {
+            const uint32_t l = q.label[k];
+            const double g = q.gain[k];
+            if (l == mine) rg = -g;
+            else if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
+                bg = g;
+                bl = l;
+            }
+        }
+        a.next[q.p[v]] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, rg, mine);
+    }
+    __syncwarp();
+}
 
 template <int G>
 __global__ void __launch_bounds__(TPB)
 k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
     constexpr int PER_WARP = 32 / G;
+    __shared__ GroupQueue queues[TPB / 32];
     const int lane = threadIdx.x & 31, gl = lane % G, g0 = lane - gl;
     const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << g0);
+    const unsigned below = (1u << lane) - 1u;
+    GroupQueue &q = queues[threadIdx.x >> 5];
     const Iv al = iv_of(a.alpha);
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t qn = 0, pend = 0;   // warp-uniform
     for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * PER_WARP < count; w += warps) {
+        if (qn > QCAP - 32) {
+            flush_queue(a, q, qn, pend, lane);
+            qn = pend = 0;
+        }
         const uint32_t slot = w * PER_WARP + lane / G;
         const bool active = slot < count;
         const uint32_t p = active ? verts[slot] : 0;
@@ -103,48 +181,49 @@ k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs 
         const uint32_t mine = active ? a.labels[p] : INVALID;
         const uint32_t gp = active ? graph_of(a, p) : 0u;
         const bool frozen = active && a.active && !a.active[gp];   // graph already converged
-        const double p_ext = a.p_ext[gp];
-        const Iv pe = iv_of(p_ext);
+        const Iv pe = iv_of(a.p_ext[gp]);
         const uint32_t l = (uint32_t)gl < deg && !frozen ? a.labels[a.adj[beg + gl]] : INVALID;
         const unsigned peers = __match_any_sync(FULL, l) & gmask;
         const bool owner = l != INVALID && lane == __ffs(peers) - 1;
         const uint32_t freq = __popc(peers);
-        // own label: exact remove gain
-        const bool own = owner && l == mine;
-        const double g_own = own ? exact_gain(a, l, freq, deg, mine, p_ext) : 0.0;
-        const unsigned own_lanes = __ballot_sync(FULL, own) & gmask;
-        const double own_val = __shfl_sync(FULL, g_own, own_lanes ? __ffs(own_lanes) - 1 : lane);
-        const double remove_gain = own_lanes ? -own_val : 0.0;
-        // foreign labels: interval first
-        const bool cand = owner && l != mine;
+        const bool own = owner && l == mine, cand = owner && l != mine;
         bool need = false;
         Iv iv = {0.f, 0.f};
-        if (cand) iv = interval_gain(a, l, freq, deg, pe, al, &need);
+        if (owner) iv = interval_any_gain(a, l, own, freq, deg, pe, al, &need);
         float m = (cand && !need) ? iv.lo : -INFINITY;
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
         const bool survive = cand && (need || (iv.hi > 0.f && iv.hi >= m));
-        double bg = 0.0;
-        uint32_t bl = INVALID;
-        if (survive) {
-            const double gx = exact_gain(a, l, freq, deg, mine, p_ext);
-            if (gx > 0.0) {
-                bg = gx;
-                bl = l;
-            }
+        const bool any_survivor = (__ballot_sync(FULL, survive) & gmask) != 0;
+        const bool item = survive || (own && (any_survivor || !own_sign_known(iv, need)));
+        const unsigned ib = __ballot_sync(FULL, item);
+        const uint32_t cnt = __popc(ib & gmask);
+        // a vertex without items: no foreign label can have a positive gain
+        const unsigned own_lanes = __ballot_sync(FULL, own) & gmask;
+        const bool own_negative = own && iv.hi < 0.f;   // remove gain > 0: leave the community
+        const bool leave = __shfl_sync(FULL, own_negative, own_lanes ? __ffs(own_lanes) - 1 : lane) && own_lanes;
+        if (active && gl == 0 && cnt == 0) a.next[p] = (!frozen && leave) ? INVALID : mine;
+        const unsigned vb = __ballot_sync(FULL, active && gl == 0 && cnt != 0);
+        const uint32_t vidx = pend + __popc(vb & below);
+        if (active && gl == 0 && cnt != 0) {
+            q.p[vidx] = p;
+            q.deg[vidx] = deg;
+            q.mine[vidx] = mine;
+            q.gp[vidx] = gp;
+            q.first[vidx] = (uint8_t)(qn + __popc(ib & ((1u << g0) - 1u)));
+            q.cnt[vidx] = (uint8_t)cnt;
         }
-#pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) {
-            const double og = __shfl_xor_sync(FULL, bg, o);
-            const uint32_t ol = __shfl_xor_sync(FULL, bl, o);
-            if (ol != INVALID && (bl == INVALID || better(og, ol, bg, bl))) {
-                bg = og;
-                bl = ol;
-            }
+        const uint32_t my_v = __shfl_sync(FULL, vidx, g0);
+        if (item) {
+            const uint32_t pos = qn + __popc(ib & below);
+            q.label[pos] = l;
+            q.freq[pos] = freq;
+            q.vert[pos] = (uint8_t)my_v;
         }
-        if (active && gl == 0)
-            a.next[p] = frozen ? mine : decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, remove_gain, mine);
+        qn += __popc(ib);
+        pend += __popc(vb);
     }
+    if (qn) flush_queue(a, q, qn, pend, lane);
 }
 
 // ---- degree > 32: one CTA per vertex, (label, count) hash table -------------
@@ -166,9 +245,12 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
                             uint32_t cap, double p_ext, Iv pe, Iv al) {
     __shared__ double s_gain[THREADS / 32];
     __shared__ uint32_t s_label[THREADS / 32];
-    __shared__ float s_lo[THREADS / 32];
+    __shared__ float s_lo[THREADS / 32], s_hi[THREADS / 32];
     __shared__ double s_remove;
     __shared__ uint32_t s_n;
+    __shared__ int s_need;        // some foreign interval was not usable
+    __shared__ int s_own;         // 0 no own label among the neighbours, 1 sign known, 2 exact needed
+    __shared__ float s_own_hi;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t beg = a.indices[p], deg = a.indices[p + 1] - beg, mine = a.labels[p];
     const uint32_t mask = cap - 1;
@@ -179,6 +261,8 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     if (threadIdx.x == 0) {
         s_remove = 0.0;
         s_n = 0;
+        s_need = 0;
+        s_own = 0;
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < deg; i += THREADS) {
@@ -203,29 +287,51 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     }
     __syncthreads();
     const uint32_t nl = s_n;
-    // pass 1: best lower bound among foreign labels
-    float m = -INFINITY;
+    // pass 1: best lower and upper bounds among foreign labels, the own label's interval
+    float m = -INFINITY, mh = -INFINITY;
     for (uint32_t i = threadIdx.x; i < nl; i += THREADS) {
         const uint32_t h = list[i], l = keys[h];
-        if (l == mine) continue;
         bool need = false;
-        const Iv iv = interval_gain(a, l, vals[h], deg, pe, al, &need);
-        if (!need) m = fmaxf(m, iv.lo);
+        const Iv iv = interval_any_gain(a, l, l == mine, vals[h], deg, pe, al, &need);
+        if (l == mine) {
+            s_own = own_sign_known(iv, need) ? 1 : 2;
+            s_own_hi = iv.hi;
+            continue;
+        }
+        if (need) s_need = 1;
+        else {
+            m = fmaxf(m, iv.lo);
+            mh = fmaxf(mh, iv.hi);
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
-    if (lane == 0) s_lo[warp] = m;
+    for (int o = 16; o > 0; o >>= 1) {
+        m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+        mh = fmaxf(mh, __shfl_xor_sync(FULL, mh, o));
+    }
+    if (lane == 0) {
+        s_lo[warp] = m;
+        s_hi[warp] = mh;
+    }
     __syncthreads();
     m = s_lo[0];
+    mh = s_hi[0];
 #pragma unroll
-    for (int w = 1; w < THREADS / 32; w++) m = fmaxf(m, s_lo[w]);
-    // pass 2: exact gains of the own label (remove gain) and of the survivors
+    for (int w = 1; w < THREADS / 32; w++) {
+        m = fmaxf(m, s_lo[w]);
+        mh = fmaxf(mh, s_hi[w]);
+    }
+    // a foreign label survives iff its interval is unusable or hi > 0 and hi >= m;
+    // the one with the largest hi decides whether any does
+    const bool any_survivor = s_need || (mh > 0.f && mh >= m);
+    // pass 2: exact gains of the survivors and, if needed, of the own label (remove gain)
     double bg = 0.0;
     uint32_t bl = INVALID;
     for (uint32_t i = threadIdx.x; i < nl; i += THREADS) {
         const uint32_t h = list[i], l = keys[h];
         if (l == mine) {
-            s_remove = -exact_gain(a, l, vals[h], deg, mine, p_ext);
+            if (any_survivor || s_own == 2) s_remove = -exact_gain(a, l, vals[h], deg, mine, p_ext);
+            else if (s_own_hi < 0.f) s_remove = 1.0;   // only its sign matters when nothing survives
             continue;
         }
         bool need = false;
@@ -354,17 +460,17 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
                   frozen_graphs ? c.b.active : nullptr, c.alpha, next};
     const DegreeClasses &k = g.cls;
     if (k.count[0]) {
-        k_improve_group<8><<<grid_for((uint64_t)k.count[0] * 8, TPB), TPB, 0, s>>>(k.list[0], k.count[0], a);
+        k_improve_group<8><<<grid_for((uint64_t)k.count[0] * 8, TPB, GROUP_GRID), TPB, 0, s>>>(k.list[0], k.count[0], a);
         CK_LAUNCH("k_improve_group8");
         c.launches++;
     }
     if (k.count[1]) {
-        k_improve_group<16><<<grid_for((uint64_t)k.count[1] * 16, TPB), TPB, 0, s>>>(k.list[1], k.count[1], a);
+        k_improve_group<16><<<grid_for((uint64_t)k.count[1] * 16, TPB, GROUP_GRID), TPB, 0, s>>>(k.list[1], k.count[1], a);
         CK_LAUNCH("k_improve_group16");
         c.launches++;
     }
     if (k.count[2]) {
-        k_improve_group<32><<<grid_for((uint64_t)k.count[2] * 32, TPB), TPB, 0, s>>>(k.list[2], k.count[2], a);
+        k_improve_group<32><<<grid_for((uint64_t)k.count[2] * 32, TPB, GROUP_GRID), TPB, 0, s>>>(k.list[2], k.count[2], a);
         CK_LAUNCH("k_improve_group32");
         c.launches++;
     }

@@ -231,21 +231,52 @@ __device__ __forceinline__ uint32_t segment_of32(const uint32_t *off, uint32_t G
     return lo - 1;
 }
 
+// Each CTA takes one contiguous range of items (loads stay coalesced: its
+// threads stride by blockDim inside the range) and a thread looks its graph up
+// only when it crosses into the next one, so per-graph totals need one atomic
+// per thread and graph met, not one per item.
+struct BlockRange {
+    uint64_t lo, hi;
+    __device__ BlockRange(uint64_t count) {
+        const uint64_t span = (count + gridDim.x - 1) / gridDim.x;
+        lo = min(count, (uint64_t)blockIdx.x * span);
+        hi = min(count, lo + span);
+    }
+};
+
 // ids of graph g span [0, gmax[g]): one past its largest id
 __global__ void k_graph_id_span(const uint32_t *__restrict__ pairs, uint64_t count, const uint64_t *__restrict__ rec_off,
                                 uint32_t G, uint32_t *gmax) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t g = segment_of(rec_off, G, i);
+    const BlockRange r(count);
+    uint32_t g = INVALID, cur = 0;
+    uint64_t end = 0;
+    for (uint64_t i = r.lo + threadIdx.x; i < r.hi; i += blockDim.x) {
+        if (g == INVALID || i >= end) {
+            if (g != INVALID) atomicMax(gmax + g, cur);
+            g = segment_of(rec_off, G, i);
+            end = rec_off[g + 1];
+            cur = 0;
+        }
         const uint32_t a = pairs[2 * i], b = pairs[2 * i + 1];
-        atomicMax(gmax + g, (a > b ? a : b) + 1);
+        cur = max(cur, (a > b ? a : b) + 1);
     }
+    if (g != INVALID) atomicMax(gmax + g, cur);
 }
 
 // disjoint id ranges: graph g's ids shifted by raw_off[g]
 __global__ void k_offset_pairs(const uint32_t *__restrict__ pairs, uint64_t count, const uint64_t *__restrict__ rec_off,
                                uint32_t G, const uint64_t *__restrict__ raw_off, uint32_t *out) {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t d = (uint32_t)raw_off[segment_of(rec_off, G, i)];
+    const BlockRange r(count);
+    uint32_t d = 0;
+    uint64_t end = 0;
+    bool have = false;
+    for (uint64_t i = r.lo + threadIdx.x; i < r.hi; i += blockDim.x) {
+        if (!have || i >= end) {
+            const uint32_t g = segment_of(rec_off, G, i);
+            end = rec_off[g + 1];
+            d = (uint32_t)raw_off[g];
+            have = true;
+        }
         out[2 * i] = pairs[2 * i] + d;
         out[2 * i + 1] = pairs[2 * i + 1] + d;
     }
@@ -254,8 +285,19 @@ __global__ void k_offset_pairs(const uint32_t *__restrict__ pairs, uint64_t coun
 // renamed vertices per graph (raw ids of graph g lie in [raw_off[g], raw_off[g+1]))
 __global__ void k_count_renamed(const uint32_t *__restrict__ rename, uint32_t n_raw, const uint64_t *__restrict__ raw_off,
                                 uint32_t G, uint32_t *ndist) {
-    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n_raw; x += gridDim.x * blockDim.x)
-        if (rename[x] != INVALID) atomicAdd(ndist + segment_of(raw_off, G, x), 1u);
+    const BlockRange r(n_raw);
+    uint32_t g = INVALID, cur = 0;
+    uint64_t end = 0;
+    for (uint64_t x = r.lo + threadIdx.x; x < r.hi; x += blockDim.x) {
+        if (g == INVALID || x >= end) {
+            if (g != INVALID && cur) atomicAdd(ndist + g, cur);
+            g = segment_of(raw_off, G, x);
+            end = raw_off[g + 1];
+            cur = 0;
+        }
+        cur += rename[x] != INVALID;
+    }
+    if (g != INVALID && cur) atomicAdd(ndist + g, cur);
 }
 
 __global__ void k_graph_of_order(const uint32_t *__restrict__ order, uint32_t n, const uint32_t *__restrict__ ren_off,
@@ -358,7 +400,7 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     if (NG > 1) {
         DevBuf<uint32_t> ndist(NG, s);
         CK(cudaMemsetAsync(ndist.get(), 0, 4 * NG, s));
-        k_count_renamed<<<grid_for(n_raw, TPB), TPB, 0, s>>>(rename.get(), n_raw, raw_off.get(), NG, ndist.get());
+        k_count_renamed<<<grid_for(n_raw, TPB, 152 * 8), TPB, 0, s>>>(rename.get(), n_raw, raw_off.get(), NG, ndist.get());
         CK_LAUNCH("k_count_renamed");
         scan_exclusive<uint32_t>((const uint32_t *)ndist.get(), ren_off.get(), NG, s);
         c.launches += 2;
@@ -409,7 +451,7 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     {
         TcPlan plan;
         tc_plan(c, o, plan, s, false);
-        count_triangles(c, o, plan, nullptr, tcount.get(), oflag.get(), s);
+        count_triangles(c, o, plan, LabelFilter{}, tcount.get(), oflag.get(), s);
     }
     DevBuf<int32_t> tri1(n1, s), tdeg1(n1, s);
     CK(cudaMemsetAsync(tdeg1.get(), 0, (size_t)n1 * 4, s));

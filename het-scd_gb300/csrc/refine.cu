@@ -18,11 +18,11 @@ constexpr unsigned TPB = 256;
 
 __global__ void __launch_bounds__(TPB)
 k_stats(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
-        const uint32_t *__restrict__ labels, Stats st) {
+        const uint32_t *__restrict__ labels, Stats st, LabelFilter skip) {
     const int lane = threadIdx.x & 31;
     for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += (gridDim.x * blockDim.x) >> 5) {
         const uint32_t l = labels[p];
-        if (l == INVALID) continue;
+        if (l == INVALID || skip.frozen(p)) continue;
         const uint32_t beg = indices[p], deg = indices[p + 1] - beg;
         uint32_t same = 0;
         for (uint32_t i = lane; i < deg; i += 32) same += labels[adj[beg + i]] == l;
@@ -41,9 +41,11 @@ k_stats(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__rest
 // internal triangle, counted from the out-slot flags of both endpoints
 __global__ void __launch_bounds__(TPB)
 k_internal_degrees(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
-                   const uint32_t *__restrict__ adj, const uint8_t *__restrict__ flag, int32_t *itdeg) {
+                   const uint32_t *__restrict__ adj, const uint8_t *__restrict__ flag, int32_t *itdeg,
+                   LabelFilter skip) {
     const int lane = threadIdx.x & 31;
     for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += (gridDim.x * blockDim.x) >> 5) {
+        if (skip.frozen(u)) continue;
         const uint32_t beg = indices[u], len = nlow[u];
         uint32_t edges = 0;
         for (uint32_t i = lane; i < len; i += 32) {
@@ -94,9 +96,10 @@ k_wcc_partial(const uint32_t *__restrict__ fin_off, const uint32_t *__restrict__
               const uint32_t *__restrict__ blk_gid, const uint32_t *__restrict__ labels, Stats st,
               const int32_t *__restrict__ tri, const int32_t *__restrict__ tri_deg,
               const uint32_t *__restrict__ itcount, const int32_t *__restrict__ itdeg, double alpha,
-              double *partial) {
+              double *partial, const uint8_t *__restrict__ active) {
     __shared__ double sh[TPB / 32];
     const uint32_t g = blk_gid[blockIdx.x];
+    if (active && !active[g]) return;   // a graph of the batch that stopped iterating
     const uint32_t end = fin_off[g + 1];
     const uint32_t base = fin_off[g] + (blockIdx.x - blk_off[g]) * WCC_CHUNK + threadIdx.x * WCC_ITEMS;
     double s = 0.0;
@@ -110,9 +113,11 @@ k_wcc_partial(const uint32_t *__restrict__ fin_off, const uint32_t *__restrict__
 // one block per graph: fixed-order sum of the graph's partials, divided by its n
 __global__ void __launch_bounds__(TPB) k_wcc_final(const double *__restrict__ partial,
                                                    const uint32_t *__restrict__ blk_off,
-                                                   const uint32_t *__restrict__ fin_off, double *out) {
+                                                   const uint32_t *__restrict__ fin_off, double *out,
+                                                   const uint8_t *__restrict__ active = nullptr) {
     __shared__ double sh[TPB / 32];
     const uint32_t g = blockIdx.x;
+    if (active && !active[g]) return;
     const uint32_t p0 = blk_off[g], parts = blk_off[g + 1] - p0, n = fin_off[g + 1] - fin_off[g];
     double s = 0.0;
     for (uint32_t i = threadIdx.x; i < parts; i += TPB) s = dadd(s, partial[p0 + i]);
@@ -330,7 +335,7 @@ void batch_reset(Ctx &c) {
     c.launches++;
 }
 
-void collect_stats(Ctx &c, const uint32_t *labels, Stats &st) {
+void collect_stats(Ctx &c, const uint32_t *labels, Stats &st, bool frozen_graphs) {
     const Graph &g = c.g;
     cudaStream_t s = c.stream;
     const size_t bytes = (size_t)(c.num_comms ? c.num_comms : 1) * 4;
@@ -339,12 +344,13 @@ void collect_stats(Ctx &c, const uint32_t *labels, Stats &st) {
     CK(cudaMemsetAsync(st.intl, 0, bytes, s));
     if (g.n == 0) return;
     PhaseScope ph(c, "stats");
-    k_stats<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.adj, labels, st);
+    const LabelFilter skip{nullptr, c.b.gid, frozen_graphs ? c.b.active : nullptr};
+    k_stats<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.adj, labels, st, skip);
     CK_LAUNCH("k_stats");
     c.launches += 1;
 }
 
-void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
+void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_graphs) {
     const Graph &g = c.g;
     cudaStream_t s = c.stream;
     if (g.n == 0) {
@@ -356,17 +362,19 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
     CK(cudaMemsetAsync(c.itcount, 0, (size_t)g.n * 4, s));
     CK(cudaMemsetAsync(c.itdeg, 0, (size_t)g.n * 4, s));
     Oriented o{g.indices, g.nlow, g.adj, g.n};
-    count_triangles(c, o, c.wplan, labels, c.itcount, c.slot_flag, s);
-    k_internal_degrees<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj,
-                                                                        c.slot_flag, c.itdeg);
-    CK_LAUNCH("k_internal_degrees");
     const Batch &b = c.b;
+    const uint8_t *active = frozen_graphs ? b.active : nullptr;
+    const LabelFilter lf{labels, b.gid, active};
+    count_triangles(c, o, c.wplan, lf, c.itcount, c.slot_flag, s);
+    k_internal_degrees<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj,
+                                                                        c.slot_flag, c.itdeg, lf);
+    CK_LAUNCH("k_internal_degrees");
     if (b.blocks) {
         k_wcc_partial<<<b.blocks, TPB, 0, s>>>(b.fin_off, b.blk_off, b.blk_gid, labels, st, g.tri, g.tri_deg,
-                                               c.itcount, c.itdeg, c.alpha, c.wcc_part);
+                                               c.itcount, c.itdeg, c.alpha, c.wcc_part, active);
         CK_LAUNCH("k_wcc_partial");
     }
-    k_wcc_final<<<b.G, TPB, 0, s>>>(c.wcc_part, b.blk_off, b.fin_off, b.wcc);
+    k_wcc_final<<<b.G, TPB, 0, s>>>(c.wcc_part, b.blk_off, b.fin_off, b.wcc, active);
     CK_LAUNCH("k_wcc_final");
     c.launches += 3;
 }

@@ -17,7 +17,8 @@
 //
 // With labels, only internal triangles count (all three vertices carry the
 // same valid label): compute_wcc's int_tri = 2 tcount and int_tri_deg = number
-// of flagged edges (src/wcc.cpp:84-127).
+// of flagged edges (src/wcc.cpp:84-127).  Only b and the table entries c with
+// a's label take part, so every hit is an internal triangle.
 //
 // Work unit = (vertex a, up to 32 consecutive b of out(a)) for one warp, or
 // (a, up to 256 b) for one CTA when out(a) is long.  out(a) is staged in a
@@ -55,11 +56,93 @@ __global__ void k_bucket_scatter(uint32_t n, InBucket f, const uint32_t *__restr
         if (f[v]) out[pos[v]] = v;
 }
 
+// Short out-lists (d+(a) <= G, G = 16 or 32): one group of G lanes per vertex
+// a, no table.  Lane i holds out(a)[i] in a register (out-lists are sorted
+// ascending); the (b, c in out(b)) items of a are flattened by a group scan
+// and taken G at a time, the owner b of an item and the position of c in
+// out(a) are both found by binary search over registers (shuffles).  Per-slot
+// hit counts go to a 32-entry shared array per warp: a hit adds one for b and
+// one for c, both entries of out(a), and flags the (b, c) slot.
+template <int G>
+__global__ void __launch_bounds__(256)
+k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, LabelFilter lf, uint32_t *tcount,
+           uint8_t *flag) {
+    constexpr int PER_WARP = 32 / G;
+    __shared__ uint32_t acc[8][32];
+    const uint32_t *labels = lf.labels;
+    const int lane = threadIdx.x & 31, gl = lane % G, g0 = lane - gl, w = threadIdx.x >> 5;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * PER_WARP; base < nverts;
+         base += warps * PER_WARP) {
+        const uint32_t vi = base + lane / G;
+        bool live = vi < nverts;
+        const uint32_t a = live ? verts[vi] : 0u;
+        uint32_t la = 0;
+        if (live && labels) {
+            la = labels[a];
+            live = la != INVALID && !lf.frozen(a);
+        }
+        const uint32_t abeg = live ? o.beg[a] : 0u, alen = live ? o.len[a] : 0u;   // alen <= G
+        const bool in_a = (uint32_t)gl < alen;
+        const uint32_t x = in_a ? o.adj[abeg + gl] : 0xffffffffu;
+        const bool ok = in_a && (!labels || labels[x] == la);   // usable as b and as c
+        const uint32_t wb = ok ? o.len[x] : 0u, bb = ok ? o.beg[x] : 0u;
+        uint32_t incl = wb;
+#pragma unroll
+        for (int d = 1; d < G; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, d, G);
+            if (gl >= d) incl += y;
+        }
+        const uint32_t total = __shfl_sync(FULL, incl, G - 1, G), pre = incl - wb;
+        uint32_t tmax = total;
+#pragma unroll
+        for (int d = G; d < 32; d <<= 1) tmax = max(tmax, __shfl_xor_sync(FULL, tmax, d));
+        acc[w][lane] = 0;
+        __syncwarp();
+        uint32_t hits = 0;
+        for (uint32_t t0 = 0; t0 < tmax; t0 += G) {
+            const uint32_t t = t0 + gl;
+            uint32_t j = 0;   // owner: last lane with pre <= t
+#pragma unroll
+            for (int st = G / 2; st > 0; st >>= 1)
+                if (__shfl_sync(FULL, pre, j + st, G) <= t) j += st;
+            const uint32_t bj = __shfl_sync(FULL, bb, j, G), pj = __shfl_sync(FULL, pre, j, G);
+            const bool valid = t < total;
+            const uint32_t cpos = bj + (t - pj);
+            const uint32_t cv = valid ? o.adj[cpos] : 0xffffffffu;
+            uint32_t k = 0;   // last entry of out(a) <= c
+#pragma unroll
+            for (int st = G / 2; st > 0; st >>= 1)
+                if (__shfl_sync(FULL, x, k + st, G) <= cv) k += st;
+            const uint32_t xk = __shfl_sync(FULL, x, k, G);        // every lane shuffles
+            const int okk = __shfl_sync(FULL, (int)ok, k, G);
+            const bool hit = valid && xk == cv && okk;
+            if (hit) {
+                atomicAdd(&acc[w][g0 + j], 1u);
+                atomicAdd(&acc[w][g0 + k], 1u);
+                flag[cpos] = 1;
+                hits++;
+            }
+        }
+        __syncwarp();
+        const uint32_t hc = acc[w][lane];
+        if (hc && in_a) {
+            atomicAdd(tcount + x, hc);
+            flag[abeg + gl] = 1;
+        }
+#pragma unroll
+        for (int d = G / 2; d > 0; d >>= 1) hits += __shfl_xor_sync(FULL, hits, d);
+        if (gl == 0 && hits) atomicAdd(tcount + a, hits);
+        __syncwarp();
+    }
+}
+
 // Warp units.  Per warp: table of TCAP (key, index) entries, LCAP counters.
 template <int WARPS, int TCAP, int LCAP, int FBITS>
 __global__ void __launch_bounds__(WARPS * 32)
 k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off, uint32_t nverts,
-          const uint32_t *__restrict__ labels, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+          LabelFilter lf, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+    const uint32_t *labels = lf.labels;
     __shared__ uint32_t filt[WARPS][(1 << FBITS) / 32];
     __shared__ uint32_t keys[WARPS][TCAP];
     __shared__ uint16_t idxs[WARPS][TCAP];
@@ -81,7 +164,7 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
         const uint32_t vi = lo - 1;
         const uint32_t a = verts[vi], ch = unit - unit_off[vi];
         const uint32_t la = labels ? labels[a] : 0u;
-        if (labels && la == INVALID) continue;
+        if (labels && (la == INVALID || lf.frozen(a))) continue;
         const uint32_t abeg = o.beg[a], alen = o.len[a];
         int bits = 1;
         while ((1u << bits) < 4 * alen) bits++;
@@ -93,6 +176,7 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
         __syncwarp();
         for (uint32_t i = lane; i < alen; i += 32) {
             const uint32_t id = o.adj[abeg + i];
+            if (labels && labels[id] != la) continue;   // only internal c can close an internal triangle
             const uint32_t hv = id * HASH_MUL, fi = hv >> (32 - FBITS);
             atomicOr(&filt[w][fi >> 5], 1u << (fi & 31));
             uint32_t h = hv >> (32 - bits);
@@ -150,7 +234,7 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
                 if (!((filt[w][fi >> 5] >> (fi & 31)) & 1u)) continue;   // certainly not in out(a)
                 uint32_t h = hv >> (32 - bits), key;
                 while ((key = keys[w][h]) != c && key != EMPTY) h = (h + 1) & tmask;
-                if (key == c && (!labels || labels[c] == la)) {
+                if (key == c) {
                     atomicAdd(&cnt[w][idxs[w][h]], 1u);
                     atomicAdd(&bhits[w][own[k]], 1u);
                     flag[cpos[k]] = 1;
@@ -180,7 +264,8 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
 template <int THREADS, int TCAP, int LCAP, int FBITS>
 __global__ void __launch_bounds__(THREADS)
 k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off, uint32_t nverts,
-         const uint32_t *__restrict__ labels, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+         LabelFilter lf, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+    const uint32_t *labels = lf.labels;
     extern __shared__ uint32_t sm[];
     uint32_t *keys = sm;                                  // TCAP
     uint32_t *cnt = sm + TCAP;                            // LCAP
@@ -204,7 +289,7 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
         const uint32_t vi = lo - 1;
         const uint32_t a = verts[vi], ch = unit - unit_off[vi];
         const uint32_t la = labels ? labels[a] : 0u;
-        if (labels && la == INVALID) {
+        if (labels && (la == INVALID || lf.frozen(a))) {
             __syncthreads();
             continue;
         }
@@ -218,6 +303,7 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < alen; i += THREADS) {
             const uint32_t id = o.adj[abeg + i];
+            if (labels && labels[id] != la) continue;   // only internal c can close an internal triangle
             const uint32_t hv = id * HASH_MUL, fi = hv >> (32 - FBITS);
             atomicOr(&filt[fi >> 5], 1u << (fi & 31));
             uint32_t h = hv >> (32 - bits);
@@ -289,7 +375,7 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
                 if (!((filt[fi >> 5] >> (fi & 31)) & 1u)) continue;   // certainly not in out(a)
                 uint32_t h = hv >> (32 - bits), key;
                 while ((key = keys[h]) != c && key != EMPTY) h = (h + 1) & tmask;
-                if (key == c && (!labels || labels[c] == la)) {
+                if (key == c) {
                     atomicAdd(&cnt[idxs[h]], 1u);
                     atomicAdd(&bhits[own[k]], 1u);
                     flag[cpos[k]] = 1;
@@ -328,7 +414,7 @@ void set_tc_attr() {
 }
 
 template <int THREADS, int TCAP, int LCAP, int FBITS>
-void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, const uint32_t *labels, uint32_t *tcount,
+void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, LabelFilter labels, uint32_t *tcount,
                    uint8_t *flag, uint32_t *ctr, unsigned grid, cudaStream_t s) {
     const size_t smem = tc_cta_smem<TCAP, LCAP, FBITS>();
     k_tc_cta<THREADS, TCAP, LCAP, FBITS><<<grid, THREADS, smem, s>>>(o, plan.verts[k], plan.unit_off[k], plan.nverts[k],
@@ -340,14 +426,15 @@ void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, const uint32_t 
 // by binary search in the sorted out-list in global memory, per-triangle
 // atomics.  Kept for generality.
 __global__ void __launch_bounds__(256)
-k_tc_huge(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, const uint32_t *__restrict__ labels,
-          uint32_t *tcount, uint8_t *flag) {
+k_tc_huge(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, LabelFilter lf, uint32_t *tcount,
+          uint8_t *flag) {
+    const uint32_t *labels = lf.labels;
     const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t vi = 0; vi < nverts; vi++) {
         const uint32_t a = verts[vi];
         const uint32_t la = labels ? labels[a] : 0u;
-        if (labels && la == INVALID) continue;
+        if (labels && (la == INVALID || lf.frozen(a))) continue;
         const uint32_t abeg = o.beg[a], alen = o.len[a];
         const uint32_t *A = o.adj + abeg;
         for (uint32_t j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < alen; j += warps) {
@@ -375,14 +462,17 @@ k_tc_huge(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, const
     }
 }
 
-// out-degree buckets: (0,64] warp units, (64,1024] and (1024,8192] CTA units, > 8192 fallback
-constexpr uint32_t B0 = 64, B1 = 1024, B2 = 8192;
+// out-degree buckets: (0,16] and (16,S] register groups (S = 0, 16 or 32), (S,B0] warp
+// units, (B0,B1] and (B1,8192] CTA units, > 8192 fallback; B0 <= 64 and B1 <= 1024
+// (the kernels' shared-memory capacities); S, B0, B1 tuned per context
+constexpr uint32_t B2 = 8192;
 
 }  // namespace
 
 void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned) {
-    const uint32_t bounds[TcPlan::K + 1] = {0, B0, B1, B2, 0xffffffffu};
-    const uint32_t per_unit[TcPlan::K] = {32, 128, 256, 1};
+    const uint32_t sm = c.tc_small, s16 = sm < 16 ? sm : 16, b0 = c.tc_b0 > sm ? c.tc_b0 : sm;
+    const uint32_t bounds[TcPlan::K + 1] = {0, s16, sm, b0, c.tc_b1, B2, 0xffffffffu};
+    const uint32_t per_unit[TcPlan::K] = {1, 1, 32, 128, 256, 1};
     for (int k = 0; k < TcPlan::K; k++) {
         DevBuf<uint32_t> pos((size_t)o.n + 1, s);
         InBucket f{o.len, bounds[k], bounds[k + 1]};
@@ -418,29 +508,95 @@ void prepare_tc_kernels() {
     done_device = dev;
 }
 
-void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, const uint32_t *labels, uint32_t *tcount,
+double autotune_tc(Ctx &c, std::vector<std::string> *report) {
+    const Graph &g = c.g;
+    cudaStream_t s = c.stream;
+    if (!c.has_graph || g.n == 0) return 0.0;
+    const Oriented o{g.indices, g.nlow, g.adj, g.n};
+    DevBuf<uint32_t> tcount(g.n, s);
+    DevBuf<uint8_t> flag(2 * (size_t)g.m + 1, s);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const uint32_t sms[] = {0, 16, 32}, b0s[] = {16, 32, 64}, b1s[] = {256, 512, 1024};
+    double best = 1e300;
+    uint32_t best_s = c.tc_small, best0 = c.tc_b0, best1 = c.tc_b1;
+    for (uint32_t sm : sms)
+        for (uint32_t b0 : b0s)
+            for (uint32_t b1 : b1s) {
+                if (b0 < sm) continue;   // (S, B0] would be empty: same plan as B0 = S
+                c.tc_small = sm;
+                c.tc_b0 = b0;
+                c.tc_b1 = b1;
+                TcPlan plan;
+                tc_plan(c, o, plan, s, false);
+                double ms_min = 1e300;
+                for (int rep = 0; rep < 2; rep++) {
+                    CK(cudaMemsetAsync(tcount.get(), 0, (size_t)g.n * 4, s));
+                    CK(cudaMemsetAsync(flag.get(), 0, 2 * (size_t)g.m, s));
+                    CK(cudaEventRecord(e0, s));
+                    count_triangles(c, o, plan, LabelFilter{}, tcount.get(), flag.get(), s);
+                    CK(cudaEventRecord(e1, s));
+                    CK(cudaEventSynchronize(e1));
+                    float ms = 0;
+                    CK(cudaEventElapsedTime(&ms, e0, e1));
+                    ms_min = ms < ms_min ? ms : ms_min;
+                }
+                if (report) {
+                    char buf[96];
+                    snprintf(buf, sizeof buf, "small<=%u warp<=%u cta<=%u: %.3f ms", sm, b0, b1, ms_min);
+                    report->push_back(buf);
+                }
+                if (ms_min < best) {
+                    best = ms_min;
+                    best_s = sm;
+                    best0 = b0;
+                    best1 = b1;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c.tc_small = best_s;
+    c.tc_b0 = best0;
+    c.tc_b1 = best1;
+    return best;
+}
+
+void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter labels, uint32_t *tcount,
                      uint8_t *flag, cudaStream_t s) {
     if (o.n == 0) return;
-    PhaseScope ph(c, labels ? "wcc_tc" : "tc");
+    PhaseScope ph(c, labels.labels ? "wcc_tc" : "tc");
     prepare_tc_kernels();
     uint32_t *ctr = c.work_counter;
     CK(cudaMemsetAsync(ctr, 0, 16, s));
     if (plan.nverts[0]) {
-        k_tc_warp<16, 256, 64, 10><<<152 * 4, 16 * 32, 0, s>>>(o, plan.verts[0], plan.unit_off[0], plan.nverts[0],
+        k_tc_small<16><<<grid_for((uint64_t)plan.nverts[0] * 16, 256, 152 * 8), 256, 0, s>>>(
+            o, plan.verts[0], plan.nverts[0], labels, tcount, flag);
+        CK_LAUNCH("k_tc_small16");
+        c.launches++;
+    }
+    if (plan.nverts[1]) {
+        k_tc_small<32><<<grid_for((uint64_t)plan.nverts[1] * 32, 256, 152 * 8), 256, 0, s>>>(
+            o, plan.verts[1], plan.nverts[1], labels, tcount, flag);
+        CK_LAUNCH("k_tc_small32");
+        c.launches++;
+    }
+    if (plan.nverts[2]) {
+        k_tc_warp<16, 256, 64, 10><<<152 * 4, 16 * 32, 0, s>>>(o, plan.verts[2], plan.unit_off[2], plan.nverts[2],
                                                            labels, tcount, flag, ctr);
         CK_LAUNCH("k_tc_warp64");
         c.launches++;
     }
-    if (plan.nverts[1]) {
-        launch_tc_cta<128, 2048, 1024, 14>(o, plan, 1, labels, tcount, flag, ctr + 1, 152 * 12, s);
-        c.launches++;
-    }
-    if (plan.nverts[2]) {
-        launch_tc_cta<256, 16384, 8192, 17>(o, plan, 2, labels, tcount, flag, ctr + 2, 152, s);
-        c.launches++;
-    }
     if (plan.nverts[3]) {
-        k_tc_huge<<<152 * 4, 256, 0, s>>>(o, plan.verts[3], plan.nverts[3], labels, tcount, flag);
+        launch_tc_cta<128, 2048, 1024, 14>(o, plan, 3, labels, tcount, flag, ctr + 1, 152 * 12, s);
+        c.launches++;
+    }
+    if (plan.nverts[4]) {
+        launch_tc_cta<256, 16384, 8192, 17>(o, plan, 4, labels, tcount, flag, ctr + 2, 152, s);
+        c.launches++;
+    }
+    if (plan.nverts[5]) {
+        k_tc_huge<<<152 * 4, 256, 0, s>>>(o, plan.verts[5], plan.nverts[5], labels, tcount, flag);
         CK_LAUNCH("k_tc_huge");
         c.launches++;
     }

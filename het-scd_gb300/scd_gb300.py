@@ -19,7 +19,7 @@ OK = 0
 ERRORS = {-1: "SCD_ERR_ARG", -2: "SCD_ERR_CUDA", -3: "SCD_ERR_OOM", -4: "SCD_ERR_STATE",
           -5: "SCD_ERR_FORMAT", -6: "SCD_ERR_TIMEOUT", -7: "SCD_ERR_LIMIT"}
 INVALID_LABEL = 0xFFFFFFFF
-FLAG_PROFILE, FLAG_PEXT_TREE = 1, 2
+FLAG_PROFILE, FLAG_PEXT_TREE, FLAG_NO_GRAPHS = 1, 2, 4
 PHASES = ("convert", "tc", "partition", "improve", "stats", "wcc_tc", "wcc")
 
 
@@ -77,6 +77,8 @@ def lib():
             "scd_batch_graph_download": ([P, u32, P, P, P, P], i32),
             "scd_batch_run": ([P, dbl, i32, P], i32),
             "scd_batch_labels": ([P, u32, P], i32),
+            "scd_autotune": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(dbl),
+                              ctypes.c_char_p, u64], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -262,6 +264,14 @@ class Engine:
         out = np.empty(max(n, 1), np.uint32)
         self._check(lib().scd_batch_labels(self._ctx, g, _p(out)))
         return out[:n]
+
+    def autotune(self):
+        sm, w, c, ms = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()
+        buf = ctypes.create_string_buffer(8192)
+        self._check(lib().scd_autotune(self._ctx, ctypes.byref(sm), ctypes.byref(w), ctypes.byref(c),
+                                       ctypes.byref(ms), buf, 8192))
+        return dict(small_max=sm.value, warp_max=w.value, cta_max=c.value, best_ms=ms.value,
+                    report=buf.value.decode().splitlines())
 
     def stream(self):
         p = ctypes.c_void_p()

@@ -40,6 +40,10 @@ extern "C" {
                                      counterpart of the event timers of src/cuda.cu:351-360 */
 #define SCD_FLAG_PEXT_TREE 2u     /* p_ext by a parallel tree sum instead of the canonical
                                      index-ordered sum (faster; may differ in the last bits) */
+#define SCD_FLAG_NO_GRAPHS 4u     /* launch every improvement iteration kernel by kernel instead
+                                     of replaying a captured CUDA graph; with SCD_FLAG_PROFILE
+                                     this times the iteration phases (captured iterations are
+                                     not split into phases) */
 
 typedef struct scd_ctx scd_ctx;
 
@@ -100,7 +104,8 @@ int scd_labels_from_device(scd_ctx *ctx, uint32_t *labels);
 
 /* Current (not best) labels and the community statistics of the current
  * labels (sizes, ext_edges, int_edges of src/scd.hpp:25-31); any pointer may be
- * NULL; arrays hold *num_communities entries. */
+ * NULL; arrays hold *num_communities entries.  Statistics are for a single graph
+ * (SCD_ERR_STATE on a batch: converged graphs of a batch stop updating theirs). */
 int scd_current_labels(scd_ctx *ctx, uint32_t *labels);
 int scd_community_stats(scd_ctx *ctx, int32_t *sizes, int32_t *ext_edges, int32_t *int_edges,
                         uint32_t *num_communities);
@@ -171,6 +176,16 @@ int scd_batch_graph_download(scd_ctx *ctx, uint32_t g, uint32_t *indices, uint32
 int scd_batch_run(scd_ctx *ctx, double threshold, int max_iters, scd_result *results);
 /* Best labels of graph g (n_g entries) in that graph's own label numbering. */
 int scd_batch_labels(scd_ctx *ctx, uint32_t g, uint32_t *labels);
+
+/* Autotuner: times the triangle-counting work split on the resident graph over
+ * a small grid and keeps the fastest for this context's later conversions and
+ * WCC passes.  The split is by out-list length: up to small_max (0, 16 or 32) a
+ * group of 16 or 32 lanes intersects in registers; up to warp_max a warp takes
+ * 32 list entries at a time against a shared-memory hash table; up to cta_max a
+ * 128-thread CTA does, longer lists go to 256-thread CTAs.  report (nullable,
+ * report_cap bytes) receives one line per candidate. */
+int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t *cta_max, double *best_ms,
+                 char *report, uint64_t report_cap);
 
 /* WCC of a labelling without any device allocation.  It has no counterpart in
  * the reference: it exists for callers that cannot let a library call
