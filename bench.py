@@ -199,7 +199,7 @@ def bench_batched(S, device, args):
     def run_group(ids):
         eng.batch_convert([graphs[i] for i in ids])
         res, rc = eng.batch_run(0.01, 1000)
-        labs = [eng.batch_labels(g) for g in range(len(ids))]
+        labs = eng.batch_labels_all()
         return res, rc, labs
 
     run_group(groups[0])                    # warm-up (allocator, module load)

@@ -76,6 +76,15 @@ __global__ void k_local_labels(uint32_t n_g, uint32_t v0, uint32_t l0, const uin
     }
 }
 
+// every graph's labels in its own numbering: l - comm_off[gid[v]]
+__global__ void k_local_labels_all(uint32_t n, const uint32_t *__restrict__ gid, const uint32_t *__restrict__ comm_off,
+                                   const uint32_t *__restrict__ labels, uint32_t *out) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t l = labels[v];
+        out[v] = l == INVALID ? INVALID : l - comm_off[gid ? gid[v] : 0u];
+    }
+}
+
 __global__ void k_gather_indices(uint32_t G, const uint32_t *__restrict__ fin_off, const uint32_t *__restrict__ indices,
                                  uint32_t *out) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x)
@@ -748,6 +757,26 @@ int scd_batch_convert(scd_ctx *ctx, const uint32_t *pairs, const uint64_t *recor
     });
 }
 
+int scd_batch_convert_lists(scd_ctx *ctx, const uint32_t *const *pairs, const uint64_t *counts,
+                            uint32_t num_graphs) {
+    return guarded(ctx, [&](Ctx &c) {
+        if (!counts || num_graphs == 0) throw Error(SCD_ERR_ARG, "no graphs");
+        std::vector<uint64_t> off(num_graphs + 1, 0);
+        for (uint32_t g = 0; g < num_graphs; g++) {
+            if (counts[g] && (!pairs || !pairs[g])) throw Error(SCD_ERR_ARG, "pairs[g] is NULL");
+            off[g + 1] = off[g] + counts[g];
+        }
+        const uint64_t count = off[num_graphs];
+        if (count >= (1ull << 31)) throw Error(SCD_ERR_LIMIT, "more than 2^31-1 edge records");
+        DevBuf<uint32_t> d(2 * count, c.stream);
+        for (uint32_t g = 0; g < num_graphs; g++)
+            if (counts[g])
+                CK(cudaMemcpyAsync(d.get() + 2 * off[g], pairs[g], 8 * counts[g], cudaMemcpyHostToDevice, c.stream));
+        convert_edges(c, d.get(), count, &off);
+        CK(cudaStreamSynchronize(c.stream));
+    });
+}
+
 int scd_batch_size(scd_ctx *ctx, uint32_t *num_graphs) {
     return guarded(ctx, [&](Ctx &c) {
         require_graph(c);
@@ -822,6 +851,25 @@ int scd_batch_labels(scd_ctx *ctx, uint32_t g, uint32_t *labels) {
         k_local_labels<<<grid_for(ng, 256), 256, 0, s>>>(ng, v0, c.b.h_comm_off[g], c.best, tmp.get());
         CK_LAUNCH("k_local_labels");
         CK(cudaMemcpyAsync(labels, tmp.get(), 4 * (size_t)ng, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    });
+}
+
+int scd_batch_labels_all(scd_ctx *ctx, uint32_t *labels, uint64_t *vertex_offsets) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_labels(c);
+        if (!labels && !vertex_offsets) throw Error(SCD_ERR_ARG, "nothing to return");
+        const Batch &b = c.b;
+        if (vertex_offsets)
+            for (uint32_t g = 0; g <= b.G; g++) vertex_offsets[g] = b.h_fin_off[g];
+        const uint32_t n = c.g.n;
+        if (!labels || n == 0) return;
+        cudaStream_t s = c.stream;
+        DevBuf<uint32_t> tmp(n, s);
+        k_local_labels_all<<<grid_for(n, 256), 256, 0, s>>>(n, b.G > 1 ? b.gid : nullptr, b.comm_off, c.best, tmp.get());
+        CK_LAUNCH("k_local_labels_all");
+        c.launches++;
+        CK(cudaMemcpyAsync(labels, tmp.get(), 4 * (size_t)n, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
     });
 }

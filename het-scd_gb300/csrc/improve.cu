@@ -226,7 +226,8 @@ k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs 
     if (qn) flush_queue(a, q, qn, pend, lane);
 }
 
-// ---- degree > 32: one CTA per vertex, (label, count) hash table -------------
+// ---- degree 33 .. 256: one warp per vertex, (label, count) hash table -------
+// ---- degree > 256: one CTA per vertex ---------------------------------------
 
 __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x ^= x >> 16;
@@ -235,6 +236,198 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
     x *= 0x846ca68bu;
     x ^= x >> 16;
     return x;
+}
+
+// One warp per vertex (degree <= WLIST): the warp's own open-addressing table
+// in shared memory and the list of its occupied entries.  Pass 1 computes every
+// label's interval (own included) and keeps each foreign upper bound in the
+// list; the exact gains needed (survivors and, if needed, the own label) are
+// queued per warp as in k_improve_group, so FP64 runs with all lanes busy.  A
+// vertex with more items than the queue holds is evaluated on its own.
+constexpr int WCAP = 512, WLIST = 256, WWARPS = 4;
+
+struct WarpTable {
+    uint32_t keys[WCAP], vals[WCAP];
+    float hi[WLIST];   // upper bound of each listed foreign label (+inf: interval unusable)
+    uint16_t list[WLIST];
+    uint32_t n;
+};
+
+__device__ __forceinline__ bool survives(float hi, float m) { return hi > 0.f && hi >= m; }
+
+__global__ void __launch_bounds__(WWARPS * 32)
+k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
+    __shared__ WarpTable tabs[WWARPS];
+    __shared__ GroupQueue queues[WWARPS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned below = (1u << lane) - 1u;
+    WarpTable &T = tabs[wid];
+    GroupQueue &q = queues[wid];
+    const Iv al = iv_of(a.alpha);
+    for (uint32_t i = lane; i < WCAP; i += 32) {
+        T.keys[i] = INVALID;
+        T.vals[i] = 0;
+    }
+    if (lane == 0) T.n = 0;
+    __syncwarp();
+    uint32_t qn = 0, pend = 0;   // warp-uniform
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t vi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; vi < count; vi += warps) {
+        const uint32_t p = verts[vi];
+        const uint32_t gp = graph_of(a, p);
+        const uint32_t mine = a.labels[p];
+        if (a.active && !a.active[gp]) {   // graph already converged: labels stay
+            if (lane == 0) a.next[p] = mine;
+            continue;
+        }
+        const uint32_t beg = a.indices[p], deg = a.indices[p + 1] - beg;
+        uint32_t cap = 64;
+        while (cap < 2 * deg) cap <<= 1;
+        const uint32_t mask = cap - 1;
+        for (uint32_t k = lane; k < deg; k += 32) {
+            const uint32_t l = a.labels[a.adj[beg + k]];
+            if (l == INVALID) continue;
+            uint32_t h = hash32(l) & mask;
+            while (true) {
+                uint32_t key = T.keys[h];
+                if (key == INVALID) {
+                    key = atomicCAS(T.keys + h, INVALID, l);
+                    if (key == INVALID) {
+                        T.list[atomicAdd(&T.n, 1u)] = (uint16_t)h;
+                        key = l;
+                    }
+                }
+                if (key == l) {
+                    atomicAdd(T.vals + h, 1u);
+                    break;
+                }
+                h = (h + 1) & mask;
+            }
+        }
+        __syncwarp();
+        const uint32_t nl = T.n;
+        const double p_ext = a.p_ext[gp];
+        const Iv pe = iv_of(p_ext);
+        // pass 1
+        float m = -INFINITY, mh = -INFINITY;
+        bool need_any = false, has_own = false, own_exact = false;
+        float own_hi = 0.f;
+        uint32_t own_f = 0;
+        for (uint32_t k = lane; k < nl; k += 32) {
+            const uint32_t h = T.list[k], l = T.keys[h], f = T.vals[h];
+            bool need = false;
+            const Iv iv = interval_any_gain(a, l, l == mine, f, deg, pe, al, &need);
+            if (l == mine) {
+                has_own = true;
+                own_exact = !own_sign_known(iv, need);
+                own_hi = iv.hi;
+                own_f = f;
+                T.hi[k] = -INFINITY;
+            } else if (need) {
+                need_any = true;
+                T.hi[k] = INFINITY;
+            } else {
+                m = fmaxf(m, iv.lo);
+                mh = fmaxf(mh, iv.hi);
+                T.hi[k] = iv.hi;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+            mh = fmaxf(mh, __shfl_xor_sync(FULL, mh, o));
+        }
+        need_any = __any_sync(FULL, need_any);
+        const unsigned own_lanes = __ballot_sync(FULL, has_own);
+        const int ol = own_lanes ? __ffs(own_lanes) - 1 : 0;
+        own_exact = __shfl_sync(FULL, own_exact, ol);
+        own_hi = __shfl_sync(FULL, own_hi, ol);
+        own_f = __shfl_sync(FULL, own_f, ol);
+        __syncwarp();
+        const bool any_survivor = need_any || (mh > 0.f && mh >= m);
+        const bool own_item = own_lanes && (own_exact || any_survivor);
+        uint32_t items = own_item ? 1u : 0u;
+        for (uint32_t kb = 0; kb < nl; kb += 32) {
+            const uint32_t k = kb + lane;
+            items += __popc(__ballot_sync(FULL, k < nl && survives(T.hi[k], m)));
+        }
+        if (items == 0) {   // no foreign label can have a positive gain
+            if (lane == 0) a.next[p] = (own_lanes && own_hi < 0.f) ? INVALID : mine;
+        } else if (items <= (uint32_t)QCAP) {
+            if (qn + items > (uint32_t)QCAP) {
+                flush_queue(a, q, qn, pend, lane);
+                qn = pend = 0;
+            }
+            uint32_t pos = qn;
+            if (own_item) {
+                if (lane == 0) {
+                    q.label[pos] = mine;
+                    q.freq[pos] = own_f;
+                    q.vert[pos] = (uint8_t)pend;
+                }
+                pos++;
+            }
+            for (uint32_t kb = 0; kb < nl; kb += 32) {
+                const uint32_t k = kb + lane;
+                const bool sv = k < nl && survives(T.hi[k], m);
+                const unsigned bal = __ballot_sync(FULL, sv);
+                if (sv) {
+                    const uint32_t at = pos + __popc(bal & below), h = T.list[k];
+                    q.label[at] = T.keys[h];
+                    q.freq[at] = T.vals[h];
+                    q.vert[at] = (uint8_t)pend;
+                }
+                pos += __popc(bal);
+            }
+            if (lane == 0) {
+                q.p[pend] = p;
+                q.deg[pend] = deg;
+                q.mine[pend] = mine;
+                q.gp[pend] = gp;
+                q.first[pend] = (uint8_t)qn;
+                q.cnt[pend] = (uint8_t)items;
+            }
+            qn += items;
+            pend++;
+            __syncwarp();
+        } else {   // more items than the queue holds: this vertex alone, lane-parallel
+            double bg = 0.0, rg = 0.0;
+            uint32_t bl = INVALID;
+            for (uint32_t k = lane; k < nl; k += 32) {
+                const uint32_t h = T.list[k], l = T.keys[h];
+                if (l == mine) {
+                    if (own_item) rg = -exact_gain(a, l, T.vals[h], deg, mine, p_ext);
+                } else if (survives(T.hi[k], m)) {
+                    const double g = exact_gain(a, l, T.vals[h], deg, mine, p_ext);
+                    if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
+                        bg = g;
+                        bl = l;
+                    }
+                }
+            }
+            rg = __shfl_sync(FULL, rg, ol);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double og = __shfl_xor_sync(FULL, bg, o);
+                const uint32_t olb = __shfl_xor_sync(FULL, bl, o);
+                if (olb != INVALID && (bl == INVALID || better(og, olb, bg, bl))) {
+                    bg = og;
+                    bl = olb;
+                }
+            }
+            if (lane == 0) a.next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, rg, mine);
+        }
+        // empty the table through its list
+        for (uint32_t k = lane; k < nl; k += 32) {
+            const uint32_t h = T.list[k];
+            T.keys[h] = INVALID;
+            T.vals[h] = 0;
+        }
+        __syncwarp();
+        if (lane == 0) T.n = 0;
+        __syncwarp();
+    }
+    if (qn) flush_queue(a, q, qn, pend, lane);
 }
 
 // One vertex per CTA.  keys/vals is an open-addressing table of cap (label,
@@ -429,7 +622,6 @@ void prepare_improve_kernels() {
     int dev = 0;
     CK(cudaGetDevice(&dev));
     if (done_device == dev) return;
-    set_cta_attr<128, 512>();
     set_cta_attr<256, 4096>();
     set_cta_attr<512, 16384>();
     done_device = dev;
@@ -475,7 +667,9 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
         c.launches++;
     }
     if (k.count[3]) {
-        launch_cta<128, 512>(k.list[3], k.count[3], a, s, 152 * 16);
+        k_improve_warp<<<grid_for((uint64_t)k.count[3] * 32, WWARPS * 32, 152 * 7), WWARPS * 32, 0, s>>>(
+            k.list[3], k.count[3], a);
+        CK_LAUNCH("k_improve_warp");
         c.launches++;
     }
     if (k.count[4]) {

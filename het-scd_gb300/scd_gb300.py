@@ -77,6 +77,8 @@ def lib():
             "scd_batch_graph_download": ([P, u32, P, P, P, P], i32),
             "scd_batch_run": ([P, dbl, i32, P], i32),
             "scd_batch_labels": ([P, u32, P], i32),
+            "scd_batch_convert_lists": ([P, P, P, u32], i32),
+            "scd_batch_labels_all": ([P, P, P], i32),
             "scd_autotune": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(dbl),
                               ctypes.c_char_p, u64], i32),
         }
@@ -222,10 +224,9 @@ class Engine:
     def batch_convert(self, graphs):
         """Device preprocessing of a list of edge lists ((E_g, 2) uint32 each)."""
         arrs = [np.ascontiguousarray(p, dtype=np.uint32).reshape(-1, 2) for p in graphs]
-        off = np.zeros(len(arrs) + 1, np.uint64)
-        off[1:] = np.cumsum([a.shape[0] for a in arrs])
-        pairs = np.concatenate(arrs) if arrs else np.zeros((0, 2), np.uint32)
-        self._check(lib().scd_batch_convert(self._ctx, _p(pairs), _p(off), len(arrs), 0))
+        ptrs = (ctypes.c_void_p * max(len(arrs), 1))(*[a.ctypes.data for a in arrs])
+        counts = np.array([a.shape[0] for a in arrs], np.uint64)
+        self._check(lib().scd_batch_convert_lists(self._ctx, ptrs, _p(counts), len(arrs)))
 
     def batch_convert_device(self, dev_ptr, record_offsets):
         off = np.ascontiguousarray(record_offsets, dtype=np.uint64)
@@ -264,6 +265,15 @@ class Engine:
         out = np.empty(max(n, 1), np.uint32)
         self._check(lib().scd_batch_labels(self._ctx, g, _p(out)))
         return out[:n]
+
+    def batch_labels_all(self):
+        """Best labels of every graph (own numbering), one array per graph."""
+        G = self.batch_size()
+        off = np.zeros(G + 1, np.uint64)
+        self._check(lib().scd_batch_labels_all(self._ctx, None, _p(off)))
+        out = np.empty(max(int(off[-1]), 1), np.uint32)
+        self._check(lib().scd_batch_labels_all(self._ctx, _p(out), None))
+        return [out[int(off[g]):int(off[g + 1])] for g in range(G)]
 
     def autotune(self):
         sm, w, c, ms = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()

@@ -121,9 +121,10 @@ class Server:
             try:
                 eng.batch_convert([r.pairs for r in batch])
                 results, rc = eng.batch_run(self.threshold, self.max_iters)
+                labels = eng.batch_labels_all()
                 for g, r in enumerate(batch):
                     r.result = results[g]
-                    r.labels = eng.batch_labels(g)
+                    r.labels = labels[g]
             except Exception as e:   # the batch fails as a whole; report it on every request
                 for r in batch:
                     r.error = e

@@ -163,6 +163,10 @@ int scd_profile_reset(scd_ctx *ctx);
  * Limits: fewer than 2^31 records and 2^32-1 distinct ids in total. */
 int scd_batch_convert(scd_ctx *ctx, const uint32_t *pairs, const uint64_t *record_offsets,
                       uint32_t num_graphs, int pairs_on_device);
+/* As scd_batch_convert from host memory, with each graph's records in its own
+ * array: counts[g] pairs at pairs[g], so callers need not concatenate them. */
+int scd_batch_convert_lists(scd_ctx *ctx, const uint32_t *const *pairs, const uint64_t *counts,
+                            uint32_t num_graphs);
 int scd_batch_size(scd_ctx *ctx, uint32_t *num_graphs);
 /* Sizes and p_ext of graph g of the batch. */
 int scd_batch_graph_info(scd_ctx *ctx, uint32_t g, uint32_t *n, uint32_t *m, double *clustering_coef);
@@ -176,6 +180,10 @@ int scd_batch_graph_download(scd_ctx *ctx, uint32_t g, uint32_t *indices, uint32
 int scd_batch_run(scd_ctx *ctx, double threshold, int max_iters, scd_result *results);
 /* Best labels of graph g (n_g entries) in that graph's own label numbering. */
 int scd_batch_labels(scd_ctx *ctx, uint32_t g, uint32_t *labels);
+/* Best labels of all graphs in one copy: graph g's n_g labels (own numbering)
+ * at labels[vertex_offsets[g] .. vertex_offsets[g+1]).  labels (nullable) holds
+ * sum n_g entries; vertex_offsets (nullable) num_graphs+1 entries. */
+int scd_batch_labels_all(scd_ctx *ctx, uint32_t *labels, uint64_t *vertex_offsets);
 
 /* Autotuner: times the triangle-counting work split on the resident graph over
  * a small grid and keeps the fastest for this context's later conversions and

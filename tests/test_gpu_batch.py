@@ -91,6 +91,17 @@ def test_each_graph_same_alone_and_in_the_batch(engine, seed):
     alone.close()
 
 
+def test_all_labels_at_once(engine):
+    graphs = [scdgen.planted(500 + 300 * i, 8.0, 0.2, 20, 60, seed=70 + i) for i in range(6)]
+    graphs.insert(3, np.zeros((0, 2), np.uint32))
+    engine.batch_convert(graphs)
+    engine.batch_run(0.01, 500)
+    every = engine.batch_labels_all()
+    assert len(every) == len(graphs)
+    for g in range(len(graphs)):
+        assert np.array_equal(every[g], engine.batch_labels(g)), g
+
+
 def test_batch_against_oracle(engine):
     graphs = [scdgen.planted(2000 + 700 * i, 10.0 + i, 0.1 + 0.05 * i, 20, 100, seed=40 + i) for i in range(5)]
     engine.batch_convert(graphs)

@@ -25,8 +25,8 @@ class FakeEngine:
             FakeEngine.live -= 1
         return [{"iterations": 1, "records": g.shape[0]} for g in self.graphs], 0
 
-    def batch_labels(self, g):
-        return np.full(self.graphs[g].shape[0], g, np.uint32)
+    def batch_labels_all(self):
+        return [np.full(p.shape[0], g, np.uint32) for g, p in enumerate(self.graphs)]
 
     def close(self):
         pass
