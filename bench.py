@@ -48,6 +48,29 @@ def algorithmic_tc_bytes(indices, adj):
     return 4 * ((n + 1) + m + s) + 8 * n, dict(n=n, m=m, merge_items=s)
 
 
+def iteration_bytes(indices, adj, labels):
+    """B_it = 4*[3(n+1) + 6*(2m) + 12n] + 12*P + B_int for one refinement iteration
+    under `labels`: P = distinct (vertex, neighbour label) pairs, B_int = 4 * sum over
+    internal edges u<v of (d_int(u) + d_int(v)).  Counted on the GPU with torch."""
+    import torch
+    dev = torch.device("cuda")
+    ind = torch.from_numpy(indices.astype("int64")).to(dev)
+    nbr = torch.from_numpy(adj.astype("int64")).to(dev)
+    lab = torch.from_numpy(labels.astype("int64")).to(dev)
+    n = ind.numel() - 1
+    deg = ind[1:] - ind[:-1]
+    src = torch.repeat_interleave(torch.arange(n, device=dev), deg)
+    lu, lv = lab[src], lab[nbr]
+    valid = lv != 0xFFFFFFFF
+    p_pairs = torch.unique(src[valid] * (1 << 32) + lv[valid]).numel()
+    same = valid & (lu == lv)
+    d_int = torch.bincount(src[same], minlength=n)
+    up = same & (src < nbr)
+    b_int = 4 * int((d_int[src[up]] + d_int[nbr[up]]).sum())
+    m2 = nbr.numel()
+    return 4 * (3 * (n + 1) + 6 * m2 + 12 * n) + 12 * p_pairs + b_int, dict(P=p_pairs, B_int=b_int)
+
+
 class ClockSampler:
     def __init__(self):
         self.rows, self.proc = [], None
@@ -94,6 +117,17 @@ def measured_peak_gbs():
         with open(p) as f:
             return float(json.load(f)["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def measured_traffic(kernel, scale):
+    """DRAM bytes (read + write) of one launch from the committed ncu summary
+    (profiles/traffic.json), scaled to R-MAT `scale` by the algorithmic bytes."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        rec = json.load(f).get(kernel, {})
+    return rec.get(f"rmat{scale}_bytes_per_launch")
 
 
 def cpu_sample_run(threads=None):
@@ -194,7 +228,7 @@ def bench_batched(S, device, args):
     groups = split_batches(sizes, args.batch_records)
     eng = S.Engine(device)
     eng.batch_convert([graphs[i] for i in groups[0]])
-    tune = eng.autotune()
+    tune = eng.autotune() if not args.no_autotune else {"small_max": None, "warp_max": None, "cta_max": None}
 
     def run_group(ids):
         eng.batch_convert([graphs[i] for i in ids])
@@ -218,6 +252,9 @@ def bench_batched(S, device, args):
     mem = eng.memory_usage()
     eng.close()
 
+    if args.loop_sample <= 0:
+        return {"graphs": k, "edges_in": records, "batches": len(groups), "graphs_per_s": k / batch_s,
+                "edges_per_s": records / batch_s, "seconds": batch_s, "gpu_launches": launches}
     step = max(1, k // args.loop_sample)
     sample = list(range(0, k, step))[: args.loop_sample]
     plain = S.Engine(device)
@@ -274,21 +311,30 @@ def _gen_request(spec):
 
 
 def bench_served(S, device, args):
-    """Open-loop Poisson arrivals at a fixed offered rate into the continuous-batching
-    server (120 GB admission budget); latency = submission to labels on the host."""
+    """The continuous-batching server (120 GB admission budget): its capacity with all
+    requests submitted at once, then open-loop Poisson arrivals at a fixed offered rate
+    (by default 75% of that capacity); latency = submission to labels on the host."""
     import numpy as np
     import serve
     specs = c5_specs(args.serve_requests)
     t0 = time.time()
     reqs = generate(_gen_request, specs)
     gen_s = time.time() - t0
-    rng = np.random.default_rng(55)
-    gaps = rng.exponential(1.0 / args.serve_rate, size=len(reqs))
-    # warm-up: every worker engine runs one small batch
     srv = serve.Server(device, workers=args.serve_workers, budget_bytes=120e9, max_batch=64)
+    # warm-up: every worker engine runs one small batch
     for r in [srv.submit(reqs[i]) for i in range(min(8, len(reqs)))]:
         r.wait(600)
+    # capacity: every request submitted at once (closed loop, batches as large as admission allows)
+    t = time.perf_counter()
+    handles = [srv.submit(p) for p in reqs]
+    for h in handles:
+        h.wait(1200)
+    capacity = len(reqs) / (max(h.finished for h in handles) - t)
+    rate = args.serve_rate if args.serve_rate > 0 else 0.75 * capacity
+    rng = np.random.default_rng(55)
+    gaps = rng.exponential(1.0 / rate, size=len(reqs))
     srv.batches.clear()
+    srv.peak_in_use = 0.0
     handles = []
     t = time.perf_counter()
     nxt = t
@@ -307,7 +353,8 @@ def bench_served(S, device, args):
     sizes = [b[0] for b in srv.batches]
     return {"workload": "Poisson arrivals; 80% planted n log-uniform [1000,50000] degree 16 mu 0.1, "
                         "20% R-MAT scale 19-21 edge factor 16",
-            "requests": len(reqs), "offered_per_s": args.serve_rate, "graphs_per_s": len(reqs) / span,
+            "requests": len(reqs), "capacity_graphs_per_s": capacity, "offered_per_s": rate,
+            "graphs_per_s": len(reqs) / span,
             "edges_per_s": sum(p.shape[0] for p in reqs) / span,
             "p50_ms": serve.percentile(lat, 50), "p99_ms": serve.percentile(lat, 99), "max_ms": max(lat),
             "workers": args.serve_workers, "budget_gb": 120, "peak_admitted_gb": srv.peak_in_use / 1e9,
@@ -323,23 +370,23 @@ def main():
     ap.add_argument("--impl", default="engine")
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the R-MAT line (profiling the other sections)")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=4096)
+    ap.add_argument("--no-autotune", action="store_true", help="batched section: keep the default split")
     ap.add_argument("--batch-records", type=int, default=1 << 28)
     ap.add_argument("--loop-sample", type=int, default=256)
     ap.add_argument("--serve-requests", type=int, default=200)
-    ap.add_argument("--serve-rate", type=float, default=40.0)
+    ap.add_argument("--serve-rate", type=float, default=0.0, help="requests/s; 0: 75%% of the measured capacity")
     ap.add_argument("--serve-workers", type=int, default=4)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
 
-    import numpy as np
     import torch
 
     import scd_gb300 as S
-    import scdgen
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -349,6 +396,24 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    line = {} if args.no_plain else bench_plain(S, args, world, rank, local, dist)
+    if not args.no_batched:
+        line["batched"] = bench_batched(S, local, args)
+    if not args.no_served:
+        line["served"] = bench_served(S, local, args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def bench_plain(S, args, world, rank, local, dist):
+    """The headline: plain SCD on one R-MAT graph, device-resident and end to end."""
+    import numpy as np
+    import torch
+
+    import scdgen
 
     t0 = time.time()
     pairs = scdgen.rmat(args.scale, 16, 0.57, 0.19, 0.19, seed=22)
@@ -431,6 +496,18 @@ def main():
     peng.close()
     peak, peak_kind = measured_peak_gbs()
     achieved = b_tc / (tc_avg / 1e3) / 1e9
+    traffic = measured_traffic("tc", args.scale)
+    # the other stages against the same peak (phase times of the kernel-by-kernel run)
+    b_pre = 16 * E + 4 * (n + 1) + 8 * m
+    pre_ms = prof["convert"][0] - prof["tc"][0]
+    b_it, itinfo = iteration_bytes(gd["indices"], gd["adj"], eng.labels_from_device())
+    it_ms = sum(prof[k][0] / max(prof[k][1], 1) for k in ("improve", "stats", "wcc"))   # one call of each
+    stages = {"preprocess_sort_csr": {"bytes": b_pre, "ms": pre_ms, "gbs": b_pre / pre_ms / 1e6},
+              "triangle_count": {"bytes": b_tc, "ms": tc_avg, "gbs": achieved},
+              "iteration": {"bytes": b_it, "ms": it_ms, "gbs": b_it / it_ms / 1e6, **itinfo,
+                            "labels": "best labels of the run"}}
+    for v in stages.values():
+        v["frac"] = v["gbs"] / peak
 
     line = {"metric": METRIC, "value": world * E / (dev_ms / 1e3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
@@ -445,7 +522,8 @@ def main():
             "roofline": {"kernel": "k_tc_warp + k_tc_cta (preprocessing triangle counting)", "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "algorithmic_bytes": b_tc, "ms_per_launch": tc_avg,
-                         "traffic": None},
+                         "traffic": traffic},
+            "stages": stages,
             "clocks": ck, "generate_s": round(gen_s, 2)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -454,15 +532,7 @@ def main():
                                 "sample": f"R-MAT scale {CPU_SAMPLE_SCALE} ({e} edges), same generator; "
                                           f"{t_ms:.0f} ms of reference-timer CPU work"}
     eng.close()
-    del dev_pairs, host_pairs
-    if not args.no_batched:
-        line["batched"] = bench_batched(S, local, args)
-    if not args.no_served:
-        line["served"] = bench_served(S, local, args)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    return line
 
 
 if __name__ == "__main__":
