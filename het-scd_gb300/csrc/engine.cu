@@ -21,12 +21,20 @@ __global__ void k_nlow(uint32_t n, const uint32_t *__restrict__ indices, const u
     }
 }
 
+struct ChunksOf {   // RowWork chunks of a long row
+    const uint32_t *verts, *indices;
+    __device__ uint32_t operator[](size_t i) const {
+        const uint32_t v = verts[i];
+        return (indices[v + 1] - indices[v] + RowWork::CHUNK - 1) / RowWork::CHUNK;
+    }
+};
+
 struct InClass {
     const uint32_t *indices;
-    uint32_t lo, hi;   // lo < deg <= hi
+    uint32_t lo, hi;   // lo <= deg <= hi
     __device__ uint32_t operator[](size_t v) const {
         const uint32_t d = indices[v + 1] - indices[v];
-        return d > lo && d <= hi;
+        return d >= lo && d <= hi;
     }
 };
 
@@ -284,10 +292,35 @@ void finish_graph(Ctx &c) {
         k_nlow<<<grid_for(n, TPB), TPB, 0, s>>>(n, g.indices, g.adj, g.nlow);
         CK_LAUNCH("k_nlow");
     }
-    uint32_t lo = 0;
+    uint32_t lo = 0;   // class 0 includes degree 0 (possible in a transferred graph; convert never keeps one)
     for (int k = 0; k < DegreeClasses::K; k++) {
         g.cls.count[k] = class_list(c, lo, DegreeClasses::upper[k], &g.cls.list[k]);
-        lo = DegreeClasses::upper[k];
+        lo = DegreeClasses::upper[k] + 1;
+    }
+    {
+        RowWork &rw = g.rows;
+        rw.l8 = g.cls.list[0];
+        rw.n8 = g.cls.count[0];
+        rw.l16 = g.cls.list[1];
+        rw.n16 = g.cls.count[1];
+        rw.l32 = g.cls.list[2];
+        rw.n32 = g.cls.count[2];
+        rw.l256 = g.cls.list[3];
+        rw.n256 = g.cls.count[3];
+        uint32_t *llong = nullptr;
+        rw.nlong = class_list(c, 257, 0xffffffffu, &llong);
+        rw.llong = llong;
+        uint32_t *coff = c.alloc<uint32_t>((size_t)rw.nlong + 1);
+        scan_exclusive<uint32_t>(ChunksOf{llong, g.indices}, coff, rw.nlong, s);
+        uint32_t chunks = 0;
+        CK(cudaMemcpyAsync(&chunks, coff + rw.nlong, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        rw.chunk_off = coff;
+        rw.e8 = (rw.n8 + 3) / 4;
+        rw.e16 = rw.e8 + (rw.n16 + 1) / 2;
+        rw.e32 = rw.e16 + rw.n32;
+        rw.e256 = rw.e32 + rw.n256;
+        rw.total = rw.e256 + chunks;
     }
     const uint32_t n_big = g.cls.count[DegreeClasses::K - 1];
     g.big_table_off = c.alloc<uint64_t>((size_t)n_big + 1);

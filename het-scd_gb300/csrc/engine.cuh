@@ -25,8 +25,20 @@ namespace scd {
 struct DegreeClasses {
     static constexpr int K = 7;
     static constexpr uint32_t upper[K] = {8, 16, 32, 256, 2048, 8192, 0xffffffffu};
-    uint32_t *list[K] = {};
+    uint32_t *list[K] = {};   // class 0 also holds the isolated vertices (degree 0)
     uint32_t count[K] = {};
+};
+
+// One launch over the rows of all vertices, as warp work units: groups of 8
+// lanes per row of degree <= 8 (4 rows per warp), 16 lanes for <= 16, a warp
+// per row up to 256, and rows longer than 256 cut into 256-entry chunks, one
+// warp each, so hub rows run alongside the rest instead of in a tail of their own.
+struct RowWork {
+    static constexpr uint32_t CHUNK = 256;
+    const uint32_t *l8 = nullptr, *l16 = nullptr, *l32 = nullptr, *l256 = nullptr, *llong = nullptr;
+    const uint32_t *chunk_off = nullptr;   // long rows: first chunk of each (nlong + 1 entries)
+    uint32_t n8 = 0, n16 = 0, n32 = 0, n256 = 0, nlong = 0;
+    uint32_t e8 = 0, e16 = 0, e32 = 0, e256 = 0, total = 0;   // ends of the warp ranges
 };
 
 struct Graph {
@@ -37,6 +49,7 @@ struct Graph {
     uint32_t max_deg = 0;
     // degree buckets of the improve kernels, built once per graph
     DegreeClasses cls;
+    RowWork rows;
     uint64_t *big_table_off = nullptr;   // hash-table offsets of the last bucket
     uint64_t big_table_words = 0;
 };

@@ -93,6 +93,23 @@ __device__ __forceinline__ Iv interval_any_gain(const ImproveArgs &a, uint32_t l
 // (remove gain > 0 exactly when the own gain is < 0).
 __device__ __forceinline__ bool own_sign_known(Iv iv, bool need) { return !need && (iv.hi < 0.f || iv.lo >= 0.f); }
 
+// The decision from intervals alone where they settle it.  b (label bl) is the
+// only foreign label that can hold the maximum gain and its lower bound is > 0
+// (so bl is the exact arg-max and the best gain bg > 0); own encloses the own
+// label's gain G (remove gain rg = -G; no own label among the neighbours: rg = 0).
+// Move if bg > G (then bg + rg > 0, and bg is far above half an ulp of rg, so
+// fl(bg + rg) > rg); stay if bg <= G (then bg + rg <= 0 and rg < 0).  Otherwise
+// the exact gains decide.
+constexpr uint32_t UNDECIDED = 0xfffffffeu;
+
+__device__ __forceinline__ uint32_t decide_iv(Iv b, uint32_t bl, bool has_own, Iv own, uint32_t mine) {
+    if (!has_own) return bl;
+    const float r = fmaxf(fabsf(own.lo), fabsf(own.hi));
+    if (b.lo > own.hi && b.lo > r * 0x1p-40f) return bl;
+    if (b.hi <= own.lo) return mine;
+    return UNDECIDED;
+}
+
 __device__ __forceinline__ uint32_t decide(double best_gain, uint32_t best_label, double remove_gain,
                                            uint32_t mine) {
     const double insert = dadd(best_gain, remove_gain);
@@ -194,15 +211,25 @@ k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs 
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
         const bool survive = cand && (need || (iv.hi > 0.f && iv.hi >= m));
-        const bool any_survivor = (__ballot_sync(FULL, survive) & gmask) != 0;
-        const bool item = survive || (own && (any_survivor || !own_sign_known(iv, need)));
+        const unsigned sb = __ballot_sync(FULL, survive) & gmask;
+        const unsigned needb = __ballot_sync(FULL, cand && need) & gmask;
+        const unsigned own_lanes = __ballot_sync(FULL, own) & gmask;
+        // one survivor whose lower bound is > 0 and above every other upper bound: try the intervals
+        const int bsrc = sb ? __ffs(sb) - 1 : lane, osrc = own_lanes ? __ffs(own_lanes) - 1 : lane;
+        const uint32_t bl = __shfl_sync(FULL, l, bsrc);
+        const Iv biv = {__shfl_sync(FULL, iv.lo, bsrc), __shfl_sync(FULL, iv.hi, bsrc)};
+        const Iv oiv = {__shfl_sync(FULL, iv.lo, osrc), __shfl_sync(FULL, iv.hi, osrc)};
+        const bool oneed = __shfl_sync(FULL, need, osrc) && own_lanes;
+        const uint32_t dec = (__popc(sb) == 1 && !needb && m > 0.f && !oneed)
+                                 ? decide_iv(biv, bl, own_lanes != 0, oiv, mine)
+                                 : UNDECIDED;
+        const bool item = dec == UNDECIDED && (survive || (own && (sb || !own_sign_known(iv, need))));
         const unsigned ib = __ballot_sync(FULL, item);
         const uint32_t cnt = __popc(ib & gmask);
-        // a vertex without items: no foreign label can have a positive gain
-        const unsigned own_lanes = __ballot_sync(FULL, own) & gmask;
-        const bool own_negative = own && iv.hi < 0.f;   // remove gain > 0: leave the community
-        const bool leave = __shfl_sync(FULL, own_negative, own_lanes ? __ffs(own_lanes) - 1 : lane) && own_lanes;
-        if (active && gl == 0 && cnt == 0) a.next[p] = (!frozen && leave) ? INVALID : mine;
+        // a vertex without items: decided by the intervals, or no foreign label can have a positive gain
+        const bool leave = own_lanes && oiv.hi < 0.f;   // remove gain > 0: leave the community
+        if (active && gl == 0 && cnt == 0)
+            a.next[p] = frozen ? mine : dec != UNDECIDED ? dec : leave ? INVALID : mine;
         const unsigned vb = __ballot_sync(FULL, active && gl == 0 && cnt != 0);
         const uint32_t vidx = pend + __popc(vb & below);
         if (active && gl == 0 && cnt != 0) {
@@ -309,9 +336,10 @@ k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a
         const double p_ext = a.p_ext[gp];
         const Iv pe = iv_of(p_ext);
         // pass 1
-        float m = -INFINITY, mh = -INFINITY;
-        bool need_any = false, has_own = false, own_exact = false;
-        float own_hi = 0.f;
+        float m = -INFINITY, mh = -INFINITY, m_hi = -INFINITY;   // m_hi: upper bound of the label holding m
+        uint32_t m_label = INVALID;
+        bool need_any = false, has_own = false, own_need = false;
+        Iv own_iv = {0.f, 0.f};
         uint32_t own_f = 0;
         for (uint32_t k = lane; k < nl; k += 32) {
             const uint32_t h = T.list[k], l = T.keys[h], f = T.vals[h];
@@ -319,40 +347,56 @@ k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a
             const Iv iv = interval_any_gain(a, l, l == mine, f, deg, pe, al, &need);
             if (l == mine) {
                 has_own = true;
-                own_exact = !own_sign_known(iv, need);
-                own_hi = iv.hi;
+                own_need = need;
+                own_iv = iv;
                 own_f = f;
                 T.hi[k] = -INFINITY;
             } else if (need) {
                 need_any = true;
                 T.hi[k] = INFINITY;
             } else {
-                m = fmaxf(m, iv.lo);
+                if (iv.lo > m) {
+                    m = iv.lo;
+                    m_hi = iv.hi;
+                    m_label = l;
+                }
                 mh = fmaxf(mh, iv.hi);
                 T.hi[k] = iv.hi;
             }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+            const float om = __shfl_xor_sync(FULL, m, o), omh = __shfl_xor_sync(FULL, m_hi, o);
+            const uint32_t oml = __shfl_xor_sync(FULL, m_label, o);
+            if (om > m || (om == m && oml < m_label)) {
+                m = om;
+                m_hi = omh;
+                m_label = oml;
+            }
             mh = fmaxf(mh, __shfl_xor_sync(FULL, mh, o));
         }
         need_any = __any_sync(FULL, need_any);
         const unsigned own_lanes = __ballot_sync(FULL, has_own);
         const int ol = own_lanes ? __ffs(own_lanes) - 1 : 0;
-        own_exact = __shfl_sync(FULL, own_exact, ol);
-        own_hi = __shfl_sync(FULL, own_hi, ol);
+        own_need = __shfl_sync(FULL, own_need, ol);
+        own_iv.lo = __shfl_sync(FULL, own_iv.lo, ol);
+        own_iv.hi = __shfl_sync(FULL, own_iv.hi, ol);
         own_f = __shfl_sync(FULL, own_f, ol);
         __syncwarp();
         const bool any_survivor = need_any || (mh > 0.f && mh >= m);
-        const bool own_item = own_lanes && (own_exact || any_survivor);
-        uint32_t items = own_item ? 1u : 0u;
+        uint32_t survivors = 0;
         for (uint32_t kb = 0; kb < nl; kb += 32) {
             const uint32_t k = kb + lane;
-            items += __popc(__ballot_sync(FULL, k < nl && survives(T.hi[k], m)));
+            survivors += __popc(__ballot_sync(FULL, k < nl && survives(T.hi[k], m)));
         }
-        if (items == 0) {   // no foreign label can have a positive gain
-            if (lane == 0) a.next[p] = (own_lanes && own_hi < 0.f) ? INVALID : mine;
+        // one survivor (it holds m) with m > 0: the intervals may settle it
+        const uint32_t dec = (survivors == 1 && !need_any && m > 0.f && !(own_lanes && own_need))
+                                 ? decide_iv(Iv{m, m_hi}, m_label, own_lanes != 0, own_iv, mine)
+                                 : UNDECIDED;
+        const bool own_item = own_lanes && (own_need || !own_sign_known(own_iv, own_need) || any_survivor);
+        const uint32_t items = dec != UNDECIDED ? 0u : survivors + (own_item ? 1u : 0u);
+        if (items == 0) {   // decided by the intervals, or no foreign label can have a positive gain
+            if (lane == 0) a.next[p] = dec != UNDECIDED ? dec : (own_lanes && own_iv.hi < 0.f) ? INVALID : mine;
         } else if (items <= (uint32_t)QCAP) {
             if (qn + items > (uint32_t)QCAP) {
                 flush_queue(a, q, qn, pend, lane);

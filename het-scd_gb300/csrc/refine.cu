@@ -16,46 +16,119 @@ constexpr unsigned TPB = 256;
 
 // ---- collect_stats ---------------------------------------------------------
 
+// The calling lane's row segment under RowWork: warp unit w, groups of G lanes.
+// live is false for slots past the end of a class list.
+struct RowSeg {
+    uint32_t v, row0, beg, end;   // vertex, start of its row, [beg, end) of the segment in adj
+    bool first, live;             // first segment of the row
+};
+
+template <int G>
+__device__ __forceinline__ RowSeg class_seg(const uint32_t *list, uint32_t count, uint32_t w,
+                                            const uint32_t *indices) {
+    const uint32_t slot = w * (32 / G) + (threadIdx.x & 31) / G;
+    RowSeg r{0u, 0u, 0u, 0u, true, slot < count};
+    if (r.live) {
+        r.v = list[slot];
+        r.row0 = r.beg = indices[r.v];
+        r.end = indices[r.v + 1];
+    }
+    return r;
+}
+
+__device__ __forceinline__ RowSeg chunk_seg(const RowWork &rw, uint32_t c, const uint32_t *indices) {
+    uint32_t lo = 0, hi = rw.nlong;   // last row whose first chunk is <= c
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rw.chunk_off[mid] <= c) lo = mid;
+        else hi = mid;
+    }
+    const uint32_t k = c - rw.chunk_off[lo];
+    RowSeg r;
+    r.v = rw.llong[lo];
+    const uint32_t b0 = indices[r.v], e0 = indices[r.v + 1];
+    r.row0 = b0;
+    r.beg = b0 + k * RowWork::CHUNK;
+    r.end = min(e0, r.beg + RowWork::CHUNK);
+    r.first = k == 0;
+    r.live = true;
+    return r;
+}
+
+// collect_stats for one row segment: sizes once per vertex, ext/int from the segment
+template <int G>
+__device__ __forceinline__ void stats_seg(RowSeg r, const uint32_t *adj, const uint32_t *labels, Stats st,
+                                          LabelFilter skip) {
+    const int gl = (threadIdx.x & 31) % G;
+    const uint32_t l = r.live ? labels[r.v] : INVALID;
+    const bool live = l != INVALID && !skip.frozen(r.v);
+    uint32_t same = 0;
+    if (live)
+        for (uint32_t i = r.beg + gl; i < r.end; i += G) same += labels[adj[i]] == l;
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) same += __shfl_xor_sync(FULL, same, o);
+    if (live && gl == 0) {
+        const uint32_t len = r.end - r.beg;
+        if (r.first) atomicAdd(st.sizes + l, 1);
+        if (len - same) atomicAdd(st.ext + l, (int)(len - same));
+        if (same) atomicAdd(st.intl + l, (int)same);
+    }
+}
+
+// collect_stats (src/scd.cpp:57-111) over the RowWork units of every row
 __global__ void __launch_bounds__(TPB)
-k_stats(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
+k_stats(RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
         const uint32_t *__restrict__ labels, Stats st, LabelFilter skip) {
-    const int lane = threadIdx.x & 31;
-    for (uint32_t p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < n; p += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t l = labels[p];
-        if (l == INVALID || skip.frozen(p)) continue;
-        const uint32_t beg = indices[p], deg = indices[p + 1] - beg;
-        uint32_t same = 0;
-        for (uint32_t i = lane; i < deg; i += 32) same += labels[adj[beg + i]] == l;
-        same = warp_sum(same);
-        if (lane == 0) {
-            atomicAdd(st.sizes + l, 1);
-            if (deg - same) atomicAdd(st.ext + l, (int)(deg - same));
-            if (same) atomicAdd(st.intl + l, (int)same);
-        }
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rw.total; w += warps) {
+        if (w < rw.e8) stats_seg<8>(class_seg<8>(rw.l8, rw.n8, w, indices), adj, labels, st, skip);
+        else if (w < rw.e16) stats_seg<16>(class_seg<16>(rw.l16, rw.n16, w - rw.e8, indices), adj, labels, st, skip);
+        else if (w < rw.e32) stats_seg<32>(class_seg<32>(rw.l32, rw.n32, w - rw.e16, indices), adj, labels, st, skip);
+        else if (w < rw.e256)
+            stats_seg<32>(class_seg<32>(rw.l256, rw.n256, w - rw.e32, indices), adj, labels, st, skip);
+        else stats_seg<32>(chunk_seg(rw, w - rw.e256, indices), adj, labels, st, skip);
     }
 }
 
 // ---- WCC ---------------------------------------------------------------------
 
-// int_tri_deg (src/wcc.cpp:124-126): per vertex, the internal edges that lie on an
-// internal triangle, counted from the out-slot flags of both endpoints
-__global__ void __launch_bounds__(TPB)
-k_internal_degrees(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
-                   const uint32_t *__restrict__ adj, const uint8_t *__restrict__ flag, int32_t *itdeg,
-                   LabelFilter skip) {
-    const int lane = threadIdx.x & 31;
-    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += (gridDim.x * blockDim.x) >> 5) {
-        if (skip.frozen(u)) continue;
-        const uint32_t beg = indices[u], len = nlow[u];
-        uint32_t edges = 0;
-        for (uint32_t i = lane; i < len; i += 32) {
-            if (flag[beg + i]) {
-                atomicAdd(itdeg + adj[beg + i], 1);
+// int_tri_deg for one row segment: its out-slots (the first nlow entries of the row)
+template <int G>
+__device__ __forceinline__ void intdeg_seg(RowSeg r, const uint32_t *nlow, const uint32_t *adj, const uint8_t *flag,
+                                           int32_t *itdeg, LabelFilter skip) {
+    const int gl = (threadIdx.x & 31) % G;
+    const bool live = r.live && !skip.frozen(r.v);
+    uint32_t edges = 0;
+    if (live) {
+        const uint32_t stop = min(r.end, r.row0 + nlow[r.v]);
+        for (uint32_t i = r.beg + gl; i < stop; i += G) {
+            if (flag[i]) {
+                atomicAdd(itdeg + adj[i], 1);
                 edges++;
             }
         }
-        edges = warp_sum(edges);
-        if (lane == 0 && edges) atomicAdd(itdeg + u, (int)edges);
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) edges += __shfl_xor_sync(FULL, edges, o);
+    if (live && gl == 0 && edges) atomicAdd(itdeg + r.v, (int)edges);
+}
+
+// int_tri_deg (src/wcc.cpp:124-126): per vertex, the internal edges that lie on an
+// internal triangle, counted from the out-slot flags of both endpoints
+__global__ void __launch_bounds__(TPB)
+k_internal_degrees(RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
+                   const uint32_t *__restrict__ adj, const uint8_t *__restrict__ flag, int32_t *itdeg,
+                   LabelFilter skip) {
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rw.total; w += warps) {
+        if (w < rw.e8) intdeg_seg<8>(class_seg<8>(rw.l8, rw.n8, w, indices), nlow, adj, flag, itdeg, skip);
+        else if (w < rw.e16)
+            intdeg_seg<16>(class_seg<16>(rw.l16, rw.n16, w - rw.e8, indices), nlow, adj, flag, itdeg, skip);
+        else if (w < rw.e32)
+            intdeg_seg<32>(class_seg<32>(rw.l32, rw.n32, w - rw.e16, indices), nlow, adj, flag, itdeg, skip);
+        else if (w < rw.e256)
+            intdeg_seg<32>(class_seg<32>(rw.l256, rw.n256, w - rw.e32, indices), nlow, adj, flag, itdeg, skip);
+        else intdeg_seg<32>(chunk_seg(rw, w - rw.e256, indices), nlow, adj, flag, itdeg, skip);
     }
 }
 
@@ -345,9 +418,9 @@ void collect_stats(Ctx &c, const uint32_t *labels, Stats &st, bool frozen_graphs
     if (g.n == 0) return;
     PhaseScope ph(c, "stats");
     const LabelFilter skip{nullptr, c.b.gid, frozen_graphs ? c.b.active : nullptr};
-    k_stats<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.adj, labels, st, skip);
+    k_stats<<<grid_for((uint64_t)g.rows.total * 32, TPB), TPB, 0, s>>>(g.rows, g.indices, g.adj, labels, st, skip);
     CK_LAUNCH("k_stats");
-    c.launches += 1;
+    c.launches++;
 }
 
 void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_graphs) {
@@ -366,8 +439,8 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_gra
     const uint8_t *active = frozen_graphs ? b.active : nullptr;
     const LabelFilter lf{labels, b.gid, active};
     count_triangles(c, o, c.wplan, lf, c.itcount, c.slot_flag, s);
-    k_internal_degrees<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj,
-                                                                        c.slot_flag, c.itdeg, lf);
+    k_internal_degrees<<<grid_for((uint64_t)g.rows.total * 32, TPB), TPB, 0, s>>>(g.rows, g.indices, g.nlow, g.adj,
+                                                                                  c.slot_flag, c.itdeg, lf);
     CK_LAUNCH("k_internal_degrees");
     if (b.blocks) {
         k_wcc_partial<<<b.blocks, TPB, 0, s>>>(b.fin_off, b.blk_off, b.blk_gid, labels, st, g.tri, g.tri_deg,

@@ -127,6 +127,27 @@ def test_empty_and_degenerate_inputs(engine):
     assert r["iterations"] >= 1
 
 
+def test_transferred_graph_with_isolated_vertices(engine):
+    """A graph file may hold vertices without edges (convert never writes one): they keep
+    their labels, count in their communities' sizes and add nothing to the WCC sum.  Their
+    clustering coefficient is 0/0 (NaN), whose place in the reference's std::sort order is
+    undefined, so the iterations start from the oracle's initial labels."""
+    g = O.Graph.from_bytes(G.graph_bytes("planted_2k_mu03"))
+    extra = 7
+    ind = np.concatenate([g.indices, np.full(extra, g.indices[-1], np.uint32)])
+    pad = np.zeros(extra, np.int32)
+    gi = O.Graph(g.n + extra, g.m, ind, g.adj, np.concatenate([g.tri, pad]), np.concatenate([g.tri_deg, pad]))
+    ref = O.run(gi, max_iters=200)
+    engine.transfer_graph(gi)
+    assert engine.graph_info()[2] == O.clustering_coef(gi)
+    engine.labels_to_device(ref["initial_labels"])
+    assert rel(engine.compute_wcc(), ref["initial_wcc"]) < WCC_RTOL
+    for i in range(len(ref["wcc"])):
+        w = engine.improve_labels()
+        assert np.array_equal(engine.current_labels(), ref["labels"][i]), f"iteration {i}"
+        assert rel(w, ref["wcc"][i]) < WCC_RTOL
+
+
 def test_call_order_and_argument_errors(engine):
     e = S.Engine(0)
     with pytest.raises(S.ScdError) as ex:
