@@ -281,6 +281,7 @@ void finish_graph(Ctx &c) {
         CK(cudaStreamSynchronize(s));
     }
     b.p_ext = c.alloc<double>(b.G);
+    b.pe32 = c.alloc<float2>(b.G);
     b.comm_off = c.alloc<uint32_t>(b.G + 1);
     b.wcc = c.alloc<double>(b.G);
     b.best_wcc = c.alloc<double>(b.G);
@@ -299,28 +300,14 @@ void finish_graph(Ctx &c) {
     }
     {
         RowWork &rw = g.rows;
-        rw.l8 = g.cls.list[0];
-        rw.n8 = g.cls.count[0];
-        rw.l16 = g.cls.list[1];
-        rw.n16 = g.cls.count[1];
-        rw.l32 = g.cls.list[2];
-        rw.n32 = g.cls.count[2];
-        rw.l256 = g.cls.list[3];
-        rw.n256 = g.cls.count[3];
         uint32_t *llong = nullptr;
-        rw.nlong = class_list(c, 257, 0xffffffffu, &llong);
+        rw.nlong = class_list(c, RowWork::CHUNK + 1, 0xffffffffu, &llong);
         rw.llong = llong;
         uint32_t *coff = c.alloc<uint32_t>((size_t)rw.nlong + 1);
         scan_exclusive<uint32_t>(ChunksOf{llong, g.indices}, coff, rw.nlong, s);
-        uint32_t chunks = 0;
-        CK(cudaMemcpyAsync(&chunks, coff + rw.nlong, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&rw.nchunks, coff + rw.nlong, 4, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         rw.chunk_off = coff;
-        rw.e8 = (rw.n8 + 3) / 4;
-        rw.e16 = rw.e8 + (rw.n16 + 1) / 2;
-        rw.e32 = rw.e16 + rw.n32;
-        rw.e256 = rw.e32 + rw.n256;
-        rw.total = rw.e256 + chunks;
     }
     const uint32_t n_big = g.cls.count[DegreeClasses::K - 1];
     g.big_table_off = c.alloc<uint64_t>((size_t)n_big + 1);

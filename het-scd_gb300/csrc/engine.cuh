@@ -29,16 +29,14 @@ struct DegreeClasses {
     uint32_t count[K] = {};
 };
 
-// One launch over the rows of all vertices, as warp work units: groups of 8
-// lanes per row of degree <= 8 (4 rows per warp), 16 lanes for <= 16, a warp
-// per row up to 256, and rows longer than 256 cut into 256-entry chunks, one
-// warp each, so hub rows run alongside the rest instead of in a tail of their own.
+// Rows longer than CHUNK cut into CHUNK-entry pieces: per-row kernels (statistics,
+// internal degrees) take one warp per short row in id order and one warp per
+// piece of a long row, so hub rows run alongside the rest instead of in a tail.
 struct RowWork {
     static constexpr uint32_t CHUNK = 256;
-    const uint32_t *l8 = nullptr, *l16 = nullptr, *l32 = nullptr, *l256 = nullptr, *llong = nullptr;
-    const uint32_t *chunk_off = nullptr;   // long rows: first chunk of each (nlong + 1 entries)
-    uint32_t n8 = 0, n16 = 0, n32 = 0, n256 = 0, nlong = 0;
-    uint32_t e8 = 0, e16 = 0, e32 = 0, e256 = 0, total = 0;   // ends of the warp ranges
+    const uint32_t *llong = nullptr;       // vertices of degree > CHUNK
+    const uint32_t *chunk_off = nullptr;   // first piece of each (nlong + 1 entries)
+    uint32_t nlong = 0, nchunks = 0;
 };
 
 struct Graph {
@@ -71,6 +69,7 @@ struct Batch {
     std::vector<uint32_t> h_m;            // undirected edges per graph
     uint32_t *gid = nullptr;              // device, n: graph of each vertex (nullptr if G == 1)
     double *p_ext = nullptr;              // device, G
+    float2 *pe32 = nullptr;               // device, G: FP32 enclosure of p_ext
     std::vector<double> h_p_ext;
     uint32_t *comm_off = nullptr;         // device, G+1 (labels of the initial partition)
     std::vector<uint32_t> h_comm_off;

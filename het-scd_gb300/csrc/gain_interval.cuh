@@ -24,9 +24,7 @@ struct Iv {
     float lo, hi;
 };
 
-__device__ __forceinline__ Iv iv_int(int k) {
-    return {__int2float_rd(k), __int2float_ru(k)};
-}
+__device__ __forceinline__ Iv iv_int(int k) { return {__int2float_rd(k), __int2float_ru(k)}; }
 __device__ __forceinline__ Iv iv_of(double x) { return {__double2float_rd(x), __double2float_ru(x)}; }
 __device__ __forceinline__ Iv iv_add(Iv a, Iv b) { return {__fadd_rd(a.lo, b.lo), __fadd_ru(a.hi, b.hi)}; }
 __device__ __forceinline__ Iv iv_sub(Iv a, Iv b) { return {__fsub_rd(a.lo, b.hi), __fsub_ru(a.hi, b.lo)}; }
@@ -41,10 +39,34 @@ __device__ __forceinline__ Iv iv_mul(Iv a, Iv b) {
     return {fminf(fminf(l1, l2), fminf(l3, l4)), fmaxf(fmaxf(h1, h2), fmaxf(h3, h4))};
 }
 
-// a / b for b not containing 0 (the caller checks): a * [1/b.hi, 1/b.lo]
-__device__ __forceinline__ Iv iv_div(Iv a, Iv b) {
-    const Iv rb = {__frcp_rd(b.hi), __frcp_ru(b.lo)};
-    return iv_mul(a, rb);
+// x moved by k ulps towards -inf / +inf (finite, nonzero x)
+__device__ __forceinline__ float ulps_down(float x, unsigned k) {
+    const unsigned u = __float_as_uint(x);
+    return __uint_as_float(x > 0.f ? u - k : u + k);
+}
+__device__ __forceinline__ float ulps_up(float x, unsigned k) {
+    const unsigned u = __float_as_uint(x);
+    return __uint_as_float(x > 0.f ? u + k : u - k);
+}
+
+// approximate reciprocal (rcp.approx.f32: at most 1 ulp from 1/x)
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// a / b for b not containing 0 (the caller checks): a * [1/b.hi, 1/b.lo], each
+// reciprocal from the approximate one widened by 2 ulps; a reciprocal that is
+// not a finite nonzero float marks the interval unusable
+__device__ __forceinline__ Iv iv_div(Iv a, Iv b, bool *bad) {
+    const float r0 = rcp_approx(b.hi), r1 = rcp_approx(b.lo);
+    const float lim = 1e37f;   // keeps the 2-ulp moves inside the finite range
+    if (!(fabsf(r0) < lim && fabsf(r1) < lim && r0 != 0.f && r1 != 0.f)) {
+        *bad = true;
+        return {0.f, 0.f};
+    }
+    return iv_mul(a, Iv{ulps_down(r0, 2), ulps_up(r1, 2)});
 }
 
 // 1: certainly > 0, -1: certainly < 0, 0: certainly == 0, 2: undecided
@@ -62,7 +84,7 @@ __device__ __forceinline__ Iv wcc_gain_iv(int r, int d_in, int d_out, int c_out,
     bool bad = false;
     const Iv dr = iv_int(r);
     const Iv zero = {0.f, 0.f}, one = {1.f, 1.f};
-    const Iv t = r > 0 ? iv_div(iv_int(c_out - d_in), dr) : zero;
+    const Iv t = r > 0 ? iv_div(iv_int(c_out - d_in), dr, &bad) : zero;
 
     const Iv din_pin = iv_mul(iv_int(imul_wrap(d_in, d_in - 1)), p_in);
     Iv den = iv_add(iv_add(din_pin, iv_mul(iv_int(imul_wrap(d_out, d_out - 1)), p_ext)),
@@ -71,7 +93,7 @@ __device__ __forceinline__ Iv wcc_gain_iv(int r, int d_in, int d_out, int c_out,
     Iv A = zero;
     int sg = iv_sign(den);
     if (sg == 2) bad = true;
-    else if (sg != 0) A = iv_div(iv_mul(din_pin, iv_int(d_in + d_out)), den);
+    else if (sg != 0) A = iv_div(iv_mul(din_pin, iv_int(d_in + d_out)), den, &bad);
 
     const Iv rr = iv_mul(iv_mul(iv_mul(iv_int(imul_wrap(r - 1, r - 2)), p_in), p_in), p_in);
     const Iv q = iv_mul(iv_int(r - 1), p_in);
@@ -86,7 +108,7 @@ __device__ __forceinline__ Iv wcc_gain_iv(int r, int d_in, int d_out, int c_out,
     Iv B = zero;
     sg = iv_sign(den);
     if (sg == 2) bad = true;
-    else if (sg != 0) B = iv_div(iv_mul(two_din, q1t), den);
+    else if (sg != 0) B = iv_div(iv_mul(two_din, q1t), den, &bad);
 
     den = iv_add(iv_add(rr, tt_pe), tr_pe);
     const Iv qt = iv_add(q, t);
@@ -101,7 +123,7 @@ __device__ __forceinline__ Iv wcc_gain_iv(int r, int d_in, int d_out, int c_out,
         const bool d1 = s1 == 1, d2 = s2 == 1;
         const bool u1 = s1 == 2, u2 = s2 == 2;
         if (u1 || u2) bad = true;
-        else if (d1 && d2) C = iv_div(iv_mul(iv_mul(iv_neg(rr), qt), alpha), den);
+        else if (d1 && d2) C = iv_div(iv_mul(iv_mul(iv_neg(rr), qt), alpha), den, &bad);
     }
     const Iv g = iv_add(iv_add(A, iv_mul(iv_int(d_in), B)), iv_mul(iv_int(r - d_in), C));
     if (!(g.lo <= g.hi)) bad = true;   // NaN bounds

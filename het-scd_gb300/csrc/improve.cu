@@ -6,17 +6,21 @@
 //                    neighbour; __match_any_sync finds equal labels (groups
 //                    are separated by a lane mask), the lowest lane of each
 //                    equal-label set owns the label;
-//   33 .. 8192       one CTA per vertex, open-addressing hash table of
-//                    (label, count) in shared memory (three sizes);
-//   > 8192           one CTA per vertex, per-vertex hash table in global memory.
-// Each distinct label other than p's own first gets an FP32 interval
-// enclosure of its FP64 gain (gain_interval.cuh).  The own label's gain (the
-// remove gain) is always evaluated exactly; a foreign label is evaluated
-// exactly only if its interval could still hold the maximum (upper bound >= the
-// best lower bound and > 0, or undecidable).  The winner is the largest exact
-// positive gain, ties to the smaller label — the candidate the reference's
-// ascending scan with a strict '>' keeps (src/scd.cpp:313-316) — and the
-// decision of src/scd.cpp:321-330 follows.  Labels update Jacobi-style.
+//   33 .. 256        one warp per vertex, open-addressing (label, count) table
+//                    in shared memory;
+//   257 .. 8192      one CTA per vertex, the table in shared memory (two sizes);
+//   > 8192           one CTA per vertex, per-vertex table in global memory.
+// Every distinct label first gets an FP32 interval enclosure of its FP64 gain
+// (gain_interval.cuh); for short label lists the intervals of many vertices are
+// evaluated together, 32 per warp pass.  The intervals settle most vertices:
+// no foreign label can have a positive gain and the own label's sign is known,
+// or exactly one foreign label can hold the maximum and it clearly beats (or
+// loses to) the own label.  Only the rest get exact FP64 gains: the foreign
+// labels whose interval could still hold the maximum and, if needed, the own
+// label (the remove gain).  The winner is the largest exact positive gain, ties
+// to the smaller label — the candidate the reference's ascending scan with a
+// strict '>' keeps (src/scd.cpp:313-316) — and the decision of
+// src/scd.cpp:321-330 follows.  Labels update Jacobi-style.
 #include "engine.cuh"
 #include "gain_interval.cuh"
 
@@ -32,6 +36,7 @@ struct ImproveArgs {
     const double *pin64;   // p_in of every community (src/scd.cpp:296-298)
     const float2 *pin32;   // its FP32 enclosure
     const double *p_ext;      // per graph
+    const float2 *pe32;       // per graph: FP32 enclosure of p_ext
     const uint32_t *gid;      // graph of each vertex (nullptr: one graph)
     const uint8_t *active;    // per graph: still iterating (nullptr: all)
     double alpha;
@@ -39,6 +44,11 @@ struct ImproveArgs {
 };
 
 __device__ __forceinline__ uint32_t graph_of(const ImproveArgs &a, uint32_t p) { return a.gid ? a.gid[p] : 0u; }
+
+__device__ __forceinline__ Iv pe_of(const ImproveArgs &a, uint32_t gp) {
+    const float2 v = a.pe32[gp];
+    return Iv{v.x, v.y};
+}
 
 __device__ __forceinline__ bool better(double g1, uint32_t l1, double g2, uint32_t l2) {
     return g1 > g2 || (g1 == g2 && l1 < l2);
@@ -76,16 +86,19 @@ __device__ __forceinline__ Iv interval_any_gain(const ImproveArgs &a, uint32_t l
                                                 uint32_t deg, Iv p_ext, Iv alpha, bool *exact_needed) {
     int size = a.st.sizes[l], ext = a.st.ext[l];
     Iv pin;
+    bool pin_bad = false;
     if (own) {
         size--;
         ext += (int)(freq - (deg - freq));
         const int in = a.st.intl[l] / 2 - (int)freq;
-        pin = size > 1 ? iv_div(iv_int(2 * in), iv_mul(iv_int(size), iv_int(size - 1))) : Iv{0.f, 0.f};
+        pin = size > 1 ? iv_div(iv_int(2 * in), iv_mul(iv_int(size), iv_int(size - 1)), &pin_bad) : Iv{0.f, 0.f};
     } else {
         const float2 p = a.pin32[l];
         pin = Iv{p.x, p.y};
     }
-    return wcc_gain_iv(size, (int)freq, (int)deg - (int)freq, ext, pin, p_ext, alpha, exact_needed);
+    const Iv g = wcc_gain_iv(size, (int)freq, (int)deg - (int)freq, ext, pin, p_ext, alpha, exact_needed);
+    *exact_needed = *exact_needed || pin_bad;
+    return g;
 }
 
 // The own label's exact gain is needed unless no foreign label survives the
@@ -128,47 +141,115 @@ __global__ void k_comm_prep(uint32_t nc, Stats st, double *pin64, float2 *pin32)
 
 // ---- degree <= G: groups of G lanes ---------------------------------------
 //
-// FP64 runs at 1/64 of the FP32 rate on this part and a warp pays for an FP64
-// instruction whatever its active lanes, so the exact gains are not evaluated
-// where they arise (one or two lanes of a group) but queued per warp: each round
-// (32/G vertices) adds at most one item per lane (the own label if its exact
-// gain is needed, every foreign survivor), and once more than QCAP-32 items wait
-// the warp evaluates them with all lanes busy, then decides every pending
-// vertex.  A vertex without items is decided at once from the intervals.
+// A group of G lanes finds the (label, frequency) pairs of its vertex with
+// __match_any_sync; the pairs go to the warp's candidate queue (below).
 
-constexpr int QCAP = 64;
 constexpr unsigned GROUP_GRID = 152 * 4;   // resident CTAs (64 registers x 256 threads): warps loop over many rounds
 
-struct GroupQueue {
-    uint32_t label[QCAP], freq[QCAP];
-    double gain[QCAP];
-    uint8_t vert[QCAP];
-    uint32_t p[QCAP], deg[QCAP], mine[QCAP], gp[QCAP];
-    uint8_t first[QCAP], cnt[QCAP];
+// Candidate queue of a warp for the group kernels: the (label, frequency) pairs
+// of the pending vertices.  The interval of every candidate is evaluated 32 at
+// a time with all lanes busy (a vertex of degree <= 32 has only a few distinct
+// labels, so evaluating them where they arise would leave most lanes idle);
+// then one lane per vertex decides from the intervals, and the rare vertices
+// that need exact gains are evaluated one at a time, lane-parallel over their
+// candidates.
+constexpr int CQ = 64;
+
+struct CandQueue {
+    uint32_t label[CQ], freq[CQ];
+    float lo[CQ], hi[CQ];
+    uint8_t vert[CQ], need[CQ];
+    uint32_t p[CQ], deg[CQ], mine[CQ], gp[CQ];   // pending vertices (each has >= 1 candidate)
+    uint8_t first[CQ], cnt[CQ], exact[CQ];
 };
 
-__device__ __forceinline__ void flush_queue(const ImproveArgs &a, GroupQueue &q, uint32_t qn, uint32_t pend,
-                                            int lane) {
+__device__ __forceinline__ void process_candidates(const ImproveArgs &a, CandQueue &q, uint32_t cn, uint32_t vn,
+                                                int lane, Iv al) {
     __syncwarp();
-    for (uint32_t i = lane; i < qn; i += 32) {
-        const uint32_t v = q.vert[i];
-        q.gain[i] = exact_gain(a, q.label[i], q.freq[i], q.deg[v], q.mine[v], a.p_ext[q.gp[v]]);
+    for (uint32_t i = lane; i < cn; i += 32) {
+        const uint32_t v = q.vert[i], l = q.label[i];
+        bool need = false;
+        const Iv iv = interval_any_gain(a, l, l == q.mine[v], q.freq[i], q.deg[v], pe_of(a, q.gp[v]), al, &need);
+        q.lo[i] = iv.lo;
+        q.hi[i] = iv.hi;
+        q.need[i] = need;
     }
     __syncwarp();
-    for (uint32_t v = lane; v < pend; v += 32) {
+    for (uint32_t v = lane; v < vn; v += 32) {
         const uint32_t mine = q.mine[v], f = q.first[v], e = f + q.cnt[v];
-        double rg = 0.0, bg = 0.0;
-        uint32_t bl = INVALID;
+        float m = -INFINITY, m_hi = -INFINITY;
+        uint32_t m_label = INVALID;
+        bool need_any = false, has_own = false, own_need = false;
+        Iv own = {0.f, 0.f};
         for (uint32_t k = f; k < e; k++) {
             const uint32_t l = q.label[k];
-            const double g = q.gain[k];
-            if (l == mine) rg = -g;
-            else if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
+            if (l == mine) {
+                has_own = true;
+                own_need = q.need[k];
+                own = Iv{q.lo[k], q.hi[k]};
+            } else if (q.need[k]) {
+                need_any = true;
+            } else if (q.lo[k] > m) {
+                m = q.lo[k];
+                m_hi = q.hi[k];
+                m_label = l;
+            }
+        }
+        uint32_t survivors = 0;
+        for (uint32_t k = f; k < e; k++)
+            survivors += q.label[k] != mine && (q.need[k] || (q.hi[k] > 0.f && q.hi[k] >= m));
+        uint32_t dec = UNDECIDED;
+        if (survivors == 1 && !need_any && m > 0.f && !(has_own && own_need))
+            dec = decide_iv(Iv{m, m_hi}, m_label, has_own, own, mine);
+        else if (survivors == 0 && !(has_own && !own_sign_known(own, own_need)))
+            dec = (has_own && own.hi < 0.f) ? INVALID : mine;   // no foreign label can have a positive gain
+        q.exact[v] = dec == UNDECIDED;
+        if (dec != UNDECIDED) a.next[q.p[v]] = dec;
+    }
+    __syncwarp();
+    // exact gains: one vertex at a time, a lane per candidate (<= 32 of them)
+    for (uint32_t v0 = 0; v0 < vn; v0 += 32) {
+        unsigned xb = __ballot_sync(FULL, v0 + lane < vn && q.exact[v0 + lane]);
+        while (xb) {
+            const uint32_t v = v0 + __ffs(xb) - 1;
+            xb &= xb - 1;
+            const uint32_t mine = q.mine[v], c = q.cnt[v], k = q.first[v] + lane;
+            const bool in = (uint32_t)lane < c;
+            const uint32_t l = in ? q.label[k] : INVALID;
+            const bool is_own = in && l == mine, need = in && q.need[k];
+            const float lo = in ? q.lo[k] : -INFINITY, hi = in ? q.hi[k] : -INFINITY;
+            float m = (in && !is_own && !need) ? lo : -INFINITY;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+            const bool survive = in && !is_own && (need || (hi > 0.f && hi >= m));
+            const bool any_survivor = __any_sync(FULL, survive);
+            const bool own_item = is_own && (any_survivor || !own_sign_known(Iv{lo, hi}, need));
+            const double p_ext = a.p_ext[q.gp[v]];
+            double g = 0.0;
+            if (survive || own_item) g = exact_gain(a, l, q.freq[k], q.deg[v], mine, p_ext);
+            const unsigned own_lanes = __ballot_sync(FULL, is_own);
+            const double own_g = __shfl_sync(FULL, g, own_lanes ? __ffs(own_lanes) - 1 : 0);
+            // remove gain: exact if evaluated; else only its sign matters (nothing survives)
+            const bool own_eval = __shfl_sync(FULL, own_item, own_lanes ? __ffs(own_lanes) - 1 : 0);
+            const float own_hi = __shfl_sync(FULL, hi, own_lanes ? __ffs(own_lanes) - 1 : 0);
+            const double rg = !own_lanes ? 0.0 : own_eval ? -own_g : (own_hi < 0.f ? 1.0 : 0.0);
+            double bg = 0.0;
+            uint32_t bl = INVALID;
+            if (survive && g > 0.0) {
                 bg = g;
                 bl = l;
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double og = __shfl_xor_sync(FULL, bg, o);
+                const uint32_t olb = __shfl_xor_sync(FULL, bl, o);
+                if (olb != INVALID && (bl == INVALID || better(og, olb, bg, bl))) {
+                    bg = og;
+                    bl = olb;
+                }
+            }
+            if (lane == 0) a.next[q.p[v]] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, rg, mine);
         }
-        a.next[q.p[v]] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, rg, mine);
     }
     __syncwarp();
 }
@@ -177,19 +258,21 @@ template <int G>
 __global__ void __launch_bounds__(TPB)
 k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
     constexpr int PER_WARP = 32 / G;
-    __shared__ GroupQueue queues[TPB / 32];
+    __shared__ CandQueue queues[TPB / 32];
     const int lane = threadIdx.x & 31, gl = lane % G, g0 = lane - gl;
     const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << g0);
     const unsigned below = (1u << lane) - 1u;
-    GroupQueue &q = queues[threadIdx.x >> 5];
+    CandQueue &q = queues[threadIdx.x >> 5];
     const Iv al = iv_of(a.alpha);
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    uint32_t qn = 0, pend = 0;   // warp-uniform
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w * PER_WARP < count; w += warps) {
-        if (qn > QCAP - 32) {
-            flush_queue(a, q, qn, pend, lane);
-            qn = pend = 0;
+    uint32_t cn = 0, vn = 0;   // warp-uniform
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;; w += warps) {
+        const bool done = w * PER_WARP >= count;
+        if (cn > CQ - 32 || (done && cn)) {   // one call site: the evaluation is inlined once
+            process_candidates(a, q, cn, vn, lane, al);
+            cn = vn = 0;
         }
+        if (done) break;
         const uint32_t slot = w * PER_WARP + lane / G;
         const bool active = slot < count;
         const uint32_t p = active ? verts[slot] : 0;
@@ -198,59 +281,34 @@ k_improve_group(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs 
         const uint32_t mine = active ? a.labels[p] : INVALID;
         const uint32_t gp = active ? graph_of(a, p) : 0u;
         const bool frozen = active && a.active && !a.active[gp];   // graph already converged
-        const Iv pe = iv_of(a.p_ext[gp]);
         const uint32_t l = (uint32_t)gl < deg && !frozen ? a.labels[a.adj[beg + gl]] : INVALID;
         const unsigned peers = __match_any_sync(FULL, l) & gmask;
         const bool owner = l != INVALID && lane == __ffs(peers) - 1;
         const uint32_t freq = __popc(peers);
-        const bool own = owner && l == mine, cand = owner && l != mine;
-        bool need = false;
-        Iv iv = {0.f, 0.f};
-        if (owner) iv = interval_any_gain(a, l, own, freq, deg, pe, al, &need);
-        float m = (cand && !need) ? iv.lo : -INFINITY;
-#pragma unroll
-        for (int o = G / 2; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
-        const bool survive = cand && (need || (iv.hi > 0.f && iv.hi >= m));
-        const unsigned sb = __ballot_sync(FULL, survive) & gmask;
-        const unsigned needb = __ballot_sync(FULL, cand && need) & gmask;
-        const unsigned own_lanes = __ballot_sync(FULL, own) & gmask;
-        // one survivor whose lower bound is > 0 and above every other upper bound: try the intervals
-        const int bsrc = sb ? __ffs(sb) - 1 : lane, osrc = own_lanes ? __ffs(own_lanes) - 1 : lane;
-        const uint32_t bl = __shfl_sync(FULL, l, bsrc);
-        const Iv biv = {__shfl_sync(FULL, iv.lo, bsrc), __shfl_sync(FULL, iv.hi, bsrc)};
-        const Iv oiv = {__shfl_sync(FULL, iv.lo, osrc), __shfl_sync(FULL, iv.hi, osrc)};
-        const bool oneed = __shfl_sync(FULL, need, osrc) && own_lanes;
-        const uint32_t dec = (__popc(sb) == 1 && !needb && m > 0.f && !oneed)
-                                 ? decide_iv(biv, bl, own_lanes != 0, oiv, mine)
-                                 : UNDECIDED;
-        const bool item = dec == UNDECIDED && (survive || (own && (sb || !own_sign_known(iv, need))));
-        const unsigned ib = __ballot_sync(FULL, item);
-        const uint32_t cnt = __popc(ib & gmask);
-        // a vertex without items: decided by the intervals, or no foreign label can have a positive gain
-        const bool leave = own_lanes && oiv.hi < 0.f;   // remove gain > 0: leave the community
-        if (active && gl == 0 && cnt == 0)
-            a.next[p] = frozen ? mine : dec != UNDECIDED ? dec : leave ? INVALID : mine;
-        const unsigned vb = __ballot_sync(FULL, active && gl == 0 && cnt != 0);
-        const uint32_t vidx = pend + __popc(vb & below);
-        if (active && gl == 0 && cnt != 0) {
+        const unsigned ob = __ballot_sync(FULL, owner);
+        const uint32_t gcnt = __popc(ob & gmask);
+        // no labelled neighbour (or the graph converged): the label stays
+        if (active && gl == 0 && gcnt == 0) a.next[p] = mine;
+        const unsigned vb = __ballot_sync(FULL, active && gl == 0 && gcnt != 0);
+        const uint32_t vidx = vn + __popc(vb & below);
+        if (active && gl == 0 && gcnt != 0) {
             q.p[vidx] = p;
             q.deg[vidx] = deg;
             q.mine[vidx] = mine;
             q.gp[vidx] = gp;
-            q.first[vidx] = (uint8_t)(qn + __popc(ib & ((1u << g0) - 1u)));
-            q.cnt[vidx] = (uint8_t)cnt;
+            q.first[vidx] = (uint8_t)(cn + __popc(ob & ((1u << g0) - 1u)));
+            q.cnt[vidx] = (uint8_t)gcnt;
         }
         const uint32_t my_v = __shfl_sync(FULL, vidx, g0);
-        if (item) {
-            const uint32_t pos = qn + __popc(ib & below);
+        if (owner) {
+            const uint32_t pos = cn + __popc(ob & below);
             q.label[pos] = l;
             q.freq[pos] = freq;
             q.vert[pos] = (uint8_t)my_v;
         }
-        qn += __popc(ib);
-        pend += __popc(vb);
+        cn += __popc(ob);
+        vn += __popc(vb);
     }
-    if (qn) flush_queue(a, q, qn, pend, lane);
 }
 
 // ---- degree 33 .. 256: one warp per vertex, (label, count) hash table -------
@@ -266,11 +324,10 @@ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
 }
 
 // One warp per vertex (degree <= WLIST): the warp's own open-addressing table
-// in shared memory and the list of its occupied entries.  Pass 1 computes every
-// label's interval (own included) and keeps each foreign upper bound in the
-// list; the exact gains needed (survivors and, if needed, the own label) are
-// queued per warp as in k_improve_group, so FP64 runs with all lanes busy.  A
-// vertex with more items than the queue holds is evaluated on its own.
+// in shared memory and the list of its occupied entries.  A vertex with at most
+// 32 distinct labels goes to the warp's candidate queue like the group kernels'
+// vertices; one with more has its intervals evaluated lane-parallel over the
+// list and, where they do not settle it, its exact gains too.
 constexpr int WCAP = 512, WLIST = 256, WWARPS = 4;
 
 struct WarpTable {
@@ -282,14 +339,107 @@ struct WarpTable {
 
 __device__ __forceinline__ bool survives(float hi, float m) { return hi > 0.f && hi >= m; }
 
+// a vertex with more than 32 distinct labels, on its own
+__device__ __forceinline__ void improve_many_labels(const ImproveArgs &a, WarpTable &T, uint32_t nl, uint32_t p,
+                                                    uint32_t gp, uint32_t mine, uint32_t deg, Iv al, int lane) {
+    const double p_ext = a.p_ext[gp];
+    const Iv pe = pe_of(a, gp);
+    float m = -INFINITY, mh = -INFINITY, m_hi = -INFINITY;   // m_hi: upper bound of the label holding m
+    uint32_t m_label = INVALID;
+    bool need_any = false, has_own = false, own_need = false;
+    Iv own_iv = {0.f, 0.f};
+    for (uint32_t k = lane; k < nl; k += 32) {
+        const uint32_t h = T.list[k], l = T.keys[h], f = T.vals[h];
+        bool need = false;
+        const Iv iv = interval_any_gain(a, l, l == mine, f, deg, pe, al, &need);
+        if (l == mine) {
+            has_own = true;
+            own_need = need;
+            own_iv = iv;
+            T.hi[k] = -INFINITY;
+        } else if (need) {
+            need_any = true;
+            T.hi[k] = INFINITY;
+        } else {
+            if (iv.lo > m) {
+                m = iv.lo;
+                m_hi = iv.hi;
+                m_label = l;
+            }
+            mh = fmaxf(mh, iv.hi);
+            T.hi[k] = iv.hi;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float om = __shfl_xor_sync(FULL, m, o), omh = __shfl_xor_sync(FULL, m_hi, o);
+        const uint32_t oml = __shfl_xor_sync(FULL, m_label, o);
+        if (om > m || (om == m && oml < m_label)) {
+            m = om;
+            m_hi = omh;
+            m_label = oml;
+        }
+        mh = fmaxf(mh, __shfl_xor_sync(FULL, mh, o));
+    }
+    need_any = __any_sync(FULL, need_any);
+    const unsigned own_lanes = __ballot_sync(FULL, has_own);
+    const int ol = own_lanes ? __ffs(own_lanes) - 1 : 0;
+    own_need = __shfl_sync(FULL, own_need, ol);
+    own_iv.lo = __shfl_sync(FULL, own_iv.lo, ol);
+    own_iv.hi = __shfl_sync(FULL, own_iv.hi, ol);
+    __syncwarp();
+    const bool any_survivor = need_any || (mh > 0.f && mh >= m);
+    uint32_t survivors = 0;
+    for (uint32_t kb = 0; kb < nl; kb += 32) {
+        const uint32_t k = kb + lane;
+        survivors += __popc(__ballot_sync(FULL, k < nl && survives(T.hi[k], m)));
+    }
+    uint32_t dec = UNDECIDED;
+    if (survivors == 1 && !need_any && m > 0.f && !(own_lanes && own_need))
+        dec = decide_iv(Iv{m, m_hi}, m_label, own_lanes != 0, own_iv, mine);
+    else if (survivors == 0 && !(own_lanes && !own_sign_known(own_iv, own_need)))
+        dec = (own_lanes && own_iv.hi < 0.f) ? INVALID : mine;
+    if (dec != UNDECIDED) {
+        if (lane == 0) a.next[p] = dec;
+        return;
+    }
+    // exact gains of the survivors and of the own label, lane-parallel over the list
+    const bool own_item = own_lanes && (own_need || !own_sign_known(own_iv, own_need) || any_survivor);
+    double bg = 0.0, rg = 0.0;
+    uint32_t bl = INVALID;
+    for (uint32_t k = lane; k < nl; k += 32) {
+        const uint32_t h = T.list[k], l = T.keys[h];
+        if (l == mine) {
+            if (own_item) rg = -exact_gain(a, l, T.vals[h], deg, mine, p_ext);
+        } else if (survives(T.hi[k], m)) {
+            const double g = exact_gain(a, l, T.vals[h], deg, mine, p_ext);
+            if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
+                bg = g;
+                bl = l;
+            }
+        }
+    }
+    rg = __shfl_sync(FULL, rg, ol);
+    if (own_lanes && !own_item) rg = own_iv.hi < 0.f ? 1.0 : 0.0;   // only its sign matters then
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double og = __shfl_xor_sync(FULL, bg, o);
+        const uint32_t olb = __shfl_xor_sync(FULL, bl, o);
+        if (olb != INVALID && (bl == INVALID || better(og, olb, bg, bl))) {
+            bg = og;
+            bl = olb;
+        }
+    }
+    if (lane == 0) a.next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, rg, mine);
+}
+
 __global__ void __launch_bounds__(WWARPS * 32)
 k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
     __shared__ WarpTable tabs[WWARPS];
-    __shared__ GroupQueue queues[WWARPS];
+    __shared__ CandQueue queues[WWARPS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const unsigned below = (1u << lane) - 1u;
     WarpTable &T = tabs[wid];
-    GroupQueue &q = queues[wid];
+    CandQueue &q = queues[wid];
     const Iv al = iv_of(a.alpha);
     for (uint32_t i = lane; i < WCAP; i += 32) {
         T.keys[i] = INVALID;
@@ -297,171 +447,78 @@ k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a
     }
     if (lane == 0) T.n = 0;
     __syncwarp();
-    uint32_t qn = 0, pend = 0;   // warp-uniform
+    uint32_t cn = 0, vn = 0;   // warp-uniform
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t vi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; vi < count; vi += warps) {
-        const uint32_t p = verts[vi];
-        const uint32_t gp = graph_of(a, p);
-        const uint32_t mine = a.labels[p];
-        if (a.active && !a.active[gp]) {   // graph already converged: labels stay
-            if (lane == 0) a.next[p] = mine;
-            continue;
+    for (uint32_t vi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;; vi += warps) {
+        const bool done = vi >= count;
+        // the label table of this vertex, before a flush needs the queue
+        uint32_t p = 0, gp = 0, mine = INVALID, deg = 0, nl = 0;
+        bool frozen = false;
+        if (!done) {
+            p = verts[vi];
+            gp = graph_of(a, p);
+            mine = a.labels[p];
+            frozen = a.active && !a.active[gp];
         }
-        const uint32_t beg = a.indices[p], deg = a.indices[p + 1] - beg;
-        uint32_t cap = 64;
-        while (cap < 2 * deg) cap <<= 1;
-        const uint32_t mask = cap - 1;
-        for (uint32_t k = lane; k < deg; k += 32) {
-            const uint32_t l = a.labels[a.adj[beg + k]];
-            if (l == INVALID) continue;
-            uint32_t h = hash32(l) & mask;
-            while (true) {
-                uint32_t key = T.keys[h];
-                if (key == INVALID) {
-                    key = atomicCAS(T.keys + h, INVALID, l);
+        if (!done && !frozen) {
+            const uint32_t beg = a.indices[p];
+            deg = a.indices[p + 1] - beg;
+            uint32_t cap = 64;
+            while (cap < 2 * deg) cap <<= 1;
+            const uint32_t mask = cap - 1;
+            for (uint32_t k = lane; k < deg; k += 32) {
+                const uint32_t l = a.labels[a.adj[beg + k]];
+                if (l == INVALID) continue;
+                uint32_t h = hash32(l) & mask;
+                while (true) {
+                    uint32_t key = T.keys[h];
                     if (key == INVALID) {
-                        T.list[atomicAdd(&T.n, 1u)] = (uint16_t)h;
-                        key = l;
+                        key = atomicCAS(T.keys + h, INVALID, l);
+                        if (key == INVALID) {
+                            T.list[atomicAdd(&T.n, 1u)] = (uint16_t)h;
+                            key = l;
+                        }
                     }
+                    if (key == l) {
+                        atomicAdd(T.vals + h, 1u);
+                        break;
+                    }
+                    h = (h + 1) & mask;
                 }
-                if (key == l) {
-                    atomicAdd(T.vals + h, 1u);
-                    break;
-                }
-                h = (h + 1) & mask;
             }
+            __syncwarp();
+            nl = T.n;
         }
-        __syncwarp();
-        const uint32_t nl = T.n;
-        const double p_ext = a.p_ext[gp];
-        const Iv pe = iv_of(p_ext);
-        // pass 1
-        float m = -INFINITY, mh = -INFINITY, m_hi = -INFINITY;   // m_hi: upper bound of the label holding m
-        uint32_t m_label = INVALID;
-        bool need_any = false, has_own = false, own_need = false;
-        Iv own_iv = {0.f, 0.f};
-        uint32_t own_f = 0;
-        for (uint32_t k = lane; k < nl; k += 32) {
-            const uint32_t h = T.list[k], l = T.keys[h], f = T.vals[h];
-            bool need = false;
-            const Iv iv = interval_any_gain(a, l, l == mine, f, deg, pe, al, &need);
-            if (l == mine) {
-                has_own = true;
-                own_need = need;
-                own_iv = iv;
-                own_f = f;
-                T.hi[k] = -INFINITY;
-            } else if (need) {
-                need_any = true;
-                T.hi[k] = INFINITY;
-            } else {
-                if (iv.lo > m) {
-                    m = iv.lo;
-                    m_hi = iv.hi;
-                    m_label = l;
-                }
-                mh = fmaxf(mh, iv.hi);
-                T.hi[k] = iv.hi;
-            }
+        const bool queued = !done && !frozen && nl > 0 && nl <= 32;
+        if ((queued && cn + nl > (uint32_t)CQ) || (done && cn)) {   // one call site
+            process_candidates(a, q, cn, vn, lane, al);
+            cn = vn = 0;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float om = __shfl_xor_sync(FULL, m, o), omh = __shfl_xor_sync(FULL, m_hi, o);
-            const uint32_t oml = __shfl_xor_sync(FULL, m_label, o);
-            if (om > m || (om == m && oml < m_label)) {
-                m = om;
-                m_hi = omh;
-                m_label = oml;
-            }
-            mh = fmaxf(mh, __shfl_xor_sync(FULL, mh, o));
-        }
-        need_any = __any_sync(FULL, need_any);
-        const unsigned own_lanes = __ballot_sync(FULL, has_own);
-        const int ol = own_lanes ? __ffs(own_lanes) - 1 : 0;
-        own_need = __shfl_sync(FULL, own_need, ol);
-        own_iv.lo = __shfl_sync(FULL, own_iv.lo, ol);
-        own_iv.hi = __shfl_sync(FULL, own_iv.hi, ol);
-        own_f = __shfl_sync(FULL, own_f, ol);
-        __syncwarp();
-        const bool any_survivor = need_any || (mh > 0.f && mh >= m);
-        uint32_t survivors = 0;
-        for (uint32_t kb = 0; kb < nl; kb += 32) {
-            const uint32_t k = kb + lane;
-            survivors += __popc(__ballot_sync(FULL, k < nl && survives(T.hi[k], m)));
-        }
-        // one survivor (it holds m) with m > 0: the intervals may settle it
-        const uint32_t dec = (survivors == 1 && !need_any && m > 0.f && !(own_lanes && own_need))
-                                 ? decide_iv(Iv{m, m_hi}, m_label, own_lanes != 0, own_iv, mine)
-                                 : UNDECIDED;
-        const bool own_item = own_lanes && (own_need || !own_sign_known(own_iv, own_need) || any_survivor);
-        const uint32_t items = dec != UNDECIDED ? 0u : survivors + (own_item ? 1u : 0u);
-        if (items == 0) {   // decided by the intervals, or no foreign label can have a positive gain
-            if (lane == 0) a.next[p] = dec != UNDECIDED ? dec : (own_lanes && own_iv.hi < 0.f) ? INVALID : mine;
-        } else if (items <= (uint32_t)QCAP) {
-            if (qn + items > (uint32_t)QCAP) {
-                flush_queue(a, q, qn, pend, lane);
-                qn = pend = 0;
-            }
-            uint32_t pos = qn;
-            if (own_item) {
-                if (lane == 0) {
-                    q.label[pos] = mine;
-                    q.freq[pos] = own_f;
-                    q.vert[pos] = (uint8_t)pend;
-                }
-                pos++;
-            }
-            for (uint32_t kb = 0; kb < nl; kb += 32) {
-                const uint32_t k = kb + lane;
-                const bool sv = k < nl && survives(T.hi[k], m);
-                const unsigned bal = __ballot_sync(FULL, sv);
-                if (sv) {
-                    const uint32_t at = pos + __popc(bal & below), h = T.list[k];
-                    q.label[at] = T.keys[h];
-                    q.freq[at] = T.vals[h];
-                    q.vert[at] = (uint8_t)pend;
-                }
-                pos += __popc(bal);
+        if (done) break;
+        if (frozen || nl == 0) {   // converged graph, or no labelled neighbour: the label stays
+            if (lane == 0) a.next[p] = mine;
+        } else if (queued) {
+            if ((uint32_t)lane < nl) {
+                const uint32_t h = T.list[lane];
+                q.label[cn + lane] = T.keys[h];
+                q.freq[cn + lane] = T.vals[h];
+                q.vert[cn + lane] = (uint8_t)vn;
             }
             if (lane == 0) {
-                q.p[pend] = p;
-                q.deg[pend] = deg;
-                q.mine[pend] = mine;
-                q.gp[pend] = gp;
-                q.first[pend] = (uint8_t)qn;
-                q.cnt[pend] = (uint8_t)items;
+                q.p[vn] = p;
+                q.deg[vn] = deg;
+                q.mine[vn] = mine;
+                q.gp[vn] = gp;
+                q.first[vn] = (uint8_t)cn;
+                q.cnt[vn] = (uint8_t)nl;
             }
-            qn += items;
-            pend++;
-            __syncwarp();
-        } else {   // more items than the queue holds: this vertex alone, lane-parallel
-            double bg = 0.0, rg = 0.0;
-            uint32_t bl = INVALID;
-            for (uint32_t k = lane; k < nl; k += 32) {
-                const uint32_t h = T.list[k], l = T.keys[h];
-                if (l == mine) {
-                    if (own_item) rg = -exact_gain(a, l, T.vals[h], deg, mine, p_ext);
-                } else if (survives(T.hi[k], m)) {
-                    const double g = exact_gain(a, l, T.vals[h], deg, mine, p_ext);
-                    if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
-                        bg = g;
-                        bl = l;
-                    }
-                }
-            }
-            rg = __shfl_sync(FULL, rg, ol);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double og = __shfl_xor_sync(FULL, bg, o);
-                const uint32_t olb = __shfl_xor_sync(FULL, bl, o);
-                if (olb != INVALID && (bl == INVALID || better(og, olb, bg, bl))) {
-                    bg = og;
-                    bl = olb;
-                }
-            }
-            if (lane == 0) a.next[p] = decide(bl == INVALID ? 0.0 : bg, bl == INVALID ? 0u : bl, rg, mine);
+            cn += nl;
+            vn++;
+        } else {
+            improve_many_labels(a, T, nl, p, gp, mine, deg, al, lane);
         }
         // empty the table through its list
+        __syncwarp();
         for (uint32_t k = lane; k < nl; k += 32) {
             const uint32_t h = T.list[k];
             T.keys[h] = INVALID;
@@ -471,7 +528,6 @@ k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a
         if (lane == 0) T.n = 0;
         __syncwarp();
     }
-    if (qn) flush_queue(a, q, qn, pend, lane);
 }
 
 // One vertex per CTA.  keys/vals is an open-addressing table of cap (label,
@@ -622,7 +678,7 @@ k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a)
         const uint32_t deg = a.indices[p + 1] - a.indices[p];
         uint32_t cap = 64;
         while (cap < 2 * deg) cap <<= 1;
-        improve_cta<THREADS>(a, p, keys, vals, list, cap, a.p_ext[gp], iv_of(a.p_ext[gp]), al);
+        improve_cta<THREADS>(a, p, keys, vals, list, cap, a.p_ext[gp], pe_of(a, gp), al);
     }
 }
 
@@ -643,7 +699,7 @@ k_improve_global(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs
         const uint64_t off = table_off[i];
         const uint32_t cap = (uint32_t)((table_off[i + 1] - off) / 3);
         uint32_t *t = tables + off;
-        improve_cta<GLOBAL_THREADS>(a, p, t, t + cap, t + 2 * cap, cap, a.p_ext[gp], iv_of(a.p_ext[gp]), al);
+        improve_cta<GLOBAL_THREADS>(a, p, t, t + cap, t + 2 * cap, cap, a.p_ext[gp], pe_of(a, gp), al);
     }
 }
 
@@ -692,7 +748,7 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
         CK_LAUNCH("k_comm_prep");
         c.launches++;
     }
-    ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.pin32, c.b.p_ext, c.b.gid,
+    ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.pin32, c.b.p_ext, c.b.pe32, c.b.gid,
                   frozen_graphs ? c.b.active : nullptr, c.alpha, next};
     const DegreeClasses &k = g.cls;
     if (k.count[0]) {

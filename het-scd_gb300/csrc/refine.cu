@@ -5,6 +5,9 @@
 // wcc: internal triangles per edge by the oriented counting kernel restricted
 // to same-label triangles, per-vertex sums, per-vertex WCC terms and a
 // fixed-order (deterministic) tree reduction.
+#include <cmath>
+#include <vector>
+
 #include "engine.cuh"
 #include "gain.cuh"
 
@@ -16,25 +19,11 @@ constexpr unsigned TPB = 256;
 
 // ---- collect_stats ---------------------------------------------------------
 
-// The calling lane's row segment under RowWork: warp unit w, groups of G lanes.
-// live is false for slots past the end of a class list.
+// A row segment for one warp: a whole short row or one piece of a long row.
 struct RowSeg {
     uint32_t v, row0, beg, end;   // vertex, start of its row, [beg, end) of the segment in adj
     bool first, live;             // first segment of the row
 };
-
-template <int G>
-__device__ __forceinline__ RowSeg class_seg(const uint32_t *list, uint32_t count, uint32_t w,
-                                            const uint32_t *indices) {
-    const uint32_t slot = w * (32 / G) + (threadIdx.x & 31) / G;
-    RowSeg r{0u, 0u, 0u, 0u, true, slot < count};
-    if (r.live) {
-        r.v = list[slot];
-        r.row0 = r.beg = indices[r.v];
-        r.end = indices[r.v + 1];
-    }
-    return r;
-}
 
 __device__ __forceinline__ RowSeg chunk_seg(const RowWork &rw, uint32_t c, const uint32_t *indices) {
     uint32_t lo = 0, hi = rw.nlong;   // last row whose first chunk is <= c
@@ -75,18 +64,26 @@ __device__ __forceinline__ void stats_seg(RowSeg r, const uint32_t *adj, const u
     }
 }
 
-// collect_stats (src/scd.cpp:57-111) over the RowWork units of every row
+// collect_stats (src/scd.cpp:57-111): one warp per vertex of degree <= 256 in id
+// order (short dependent-load chains, consecutive warps on consecutive rows),
+// the rows longer than 256 as RowWork chunks after them
 __global__ void __launch_bounds__(TPB)
-k_stats(RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
+k_stats(uint32_t n, RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
         const uint32_t *__restrict__ labels, Stats st, LabelFilter skip) {
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rw.total; w += warps) {
-        if (w < rw.e8) stats_seg<8>(class_seg<8>(rw.l8, rw.n8, w, indices), adj, labels, st, skip);
-        else if (w < rw.e16) stats_seg<16>(class_seg<16>(rw.l16, rw.n16, w - rw.e8, indices), adj, labels, st, skip);
-        else if (w < rw.e32) stats_seg<32>(class_seg<32>(rw.l32, rw.n32, w - rw.e16, indices), adj, labels, st, skip);
-        else if (w < rw.e256)
-            stats_seg<32>(class_seg<32>(rw.l256, rw.n256, w - rw.e32, indices), adj, labels, st, skip);
-        else stats_seg<32>(chunk_seg(rw, w - rw.e256, indices), adj, labels, st, skip);
+    const uint32_t nchunks = rw.nchunks;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n + nchunks; w += warps) {
+        RowSeg r;
+        if (w < n) {
+            r.v = w;
+            r.row0 = r.beg = indices[w];
+            r.end = indices[w + 1];
+            r.first = true;
+            r.live = r.end - r.beg <= RowWork::CHUNK;
+        } else {
+            r = chunk_seg(rw, w - n, indices);
+        }
+        stats_seg<32>(r, adj, labels, st, skip);
     }
 }
 
@@ -115,20 +112,27 @@ __device__ __forceinline__ void intdeg_seg(RowSeg r, const uint32_t *nlow, const
 
 // int_tri_deg (src/wcc.cpp:124-126): per vertex, the internal edges that lie on an
 // internal triangle, counted from the out-slot flags of both endpoints
+// int_tri_deg (src/wcc.cpp:124-126): per vertex, the internal edges that lie on an
+// internal triangle, counted from the out-slot flags of both endpoints; one warp
+// per vertex of degree <= 256 in id order, longer rows as RowWork chunks
 __global__ void __launch_bounds__(TPB)
-k_internal_degrees(RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
+k_internal_degrees(uint32_t n, RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
                    const uint32_t *__restrict__ adj, const uint8_t *__restrict__ flag, int32_t *itdeg,
                    LabelFilter skip) {
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < rw.total; w += warps) {
-        if (w < rw.e8) intdeg_seg<8>(class_seg<8>(rw.l8, rw.n8, w, indices), nlow, adj, flag, itdeg, skip);
-        else if (w < rw.e16)
-            intdeg_seg<16>(class_seg<16>(rw.l16, rw.n16, w - rw.e8, indices), nlow, adj, flag, itdeg, skip);
-        else if (w < rw.e32)
-            intdeg_seg<32>(class_seg<32>(rw.l32, rw.n32, w - rw.e16, indices), nlow, adj, flag, itdeg, skip);
-        else if (w < rw.e256)
-            intdeg_seg<32>(class_seg<32>(rw.l256, rw.n256, w - rw.e32, indices), nlow, adj, flag, itdeg, skip);
-        else intdeg_seg<32>(chunk_seg(rw, w - rw.e256, indices), nlow, adj, flag, itdeg, skip);
+    const uint32_t nchunks = rw.nchunks;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n + nchunks; w += warps) {
+        RowSeg r;
+        if (w < n) {
+            r.v = w;
+            r.row0 = r.beg = indices[w];
+            r.end = indices[w + 1];
+            r.first = true;
+            r.live = r.end - r.beg <= RowWork::CHUNK;
+        } else {
+            r = chunk_seg(rw, w - n, indices);
+        }
+        intdeg_seg<32>(r, nlow, adj, flag, itdeg, skip);
     }
 }
 
@@ -418,7 +422,8 @@ void collect_stats(Ctx &c, const uint32_t *labels, Stats &st, bool frozen_graphs
     if (g.n == 0) return;
     PhaseScope ph(c, "stats");
     const LabelFilter skip{nullptr, c.b.gid, frozen_graphs ? c.b.active : nullptr};
-    k_stats<<<grid_for((uint64_t)g.rows.total * 32, TPB), TPB, 0, s>>>(g.rows, g.indices, g.adj, labels, st, skip);
+    k_stats<<<grid_for(((uint64_t)g.n + g.rows.nchunks) * 32, TPB), TPB, 0, s>>>(g.n, g.rows, g.indices,
+                                                                                          g.adj, labels, st, skip);
     CK_LAUNCH("k_stats");
     c.launches++;
 }
@@ -439,8 +444,8 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_gra
     const uint8_t *active = frozen_graphs ? b.active : nullptr;
     const LabelFilter lf{labels, b.gid, active};
     count_triangles(c, o, c.wplan, lf, c.itcount, c.slot_flag, s);
-    k_internal_degrees<<<grid_for((uint64_t)g.rows.total * 32, TPB), TPB, 0, s>>>(g.rows, g.indices, g.nlow, g.adj,
-                                                                                  c.slot_flag, c.itdeg, lf);
+    k_internal_degrees<<<grid_for(((uint64_t)g.n + g.rows.nchunks) * 32, TPB), TPB, 0, s>>>(
+        g.n, g.rows, g.indices, g.nlow, g.adj, c.slot_flag, c.itdeg, lf);
     CK_LAUNCH("k_internal_degrees");
     if (b.blocks) {
         k_wcc_partial<<<b.blocks, TPB, 0, s>>>(b.fin_off, b.blk_off, b.blk_gid, labels, st, g.tri, g.tri_deg,
@@ -488,6 +493,16 @@ void compute_p_ext(Ctx &c) {
     CK(cudaMemcpyAsync(b.h_p_ext.data(), b.p_ext, sizeof(double) * b.G, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     g.p_ext = b.h_p_ext[0];
+    // FP32 enclosure of every p_ext for the interval gains
+    std::vector<float2> pe(b.G);
+    for (uint32_t i = 0; i < b.G; i++) {
+        const double d = b.h_p_ext[i];
+        const float f = (float)d;
+        pe[i] = make_float2((double)f > d ? std::nextafter(f, -INFINITY) : f,
+                            (double)f < d ? std::nextafter(f, INFINITY) : f);
+    }
+    CK(cudaMemcpyAsync(b.pe32, pe.data(), sizeof(float2) * b.G, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
 }
 
 }  // namespace scd
