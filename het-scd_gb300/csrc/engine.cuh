@@ -129,6 +129,11 @@ struct Ctx;
 void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned);
 // tcount[v] += triangles at v; flag[slot] = 1 for out-slots on a triangle.
 // With labels: internal triangles only.  tcount and flag must be zeroed.
+// Sorts every row of a CSR (offsets off[nrows+1], values vals) ascending in place;
+// with dedup, repeated values of a row become INVALID and udeg[r] receives the
+// number of distinct values of row r.
+void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool dedup, uint32_t *udeg,
+               cudaStream_t s);
 void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter labels, uint32_t *tcount,
                      uint8_t *flag, cudaStream_t s);
 // times the triangle-counting bucket splits on the resident graph, keeps the fastest

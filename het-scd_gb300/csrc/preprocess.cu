@@ -4,15 +4,16 @@
 //  1. first-appearance renumbering (src/convert.cpp:141-170): first position of
 //     every raw id (atomicMin over the 2E endpoint slots), a bitmap of those
 //     positions and a popcount prefix give each id its rank of first appearance;
-//  2. both directions of every renamed non-loop pair as one 2k-bit key
-//     (row << k | col), one stable LSD radix sort, adjacent duplicates dropped:
+//  2. both directions of every renamed non-loop pair placed by a counting sort
+//     on the row, every row sorted and its repeated values dropped (csr.cu):
 //     the de-duplicated symmetric CSR (src/convert.cpp:252-268 + 417-463);
 //  3. degree orientation (u -> v iff (deg v, v) > (deg u, u)), triangles per
 //     vertex and "edge lies on a triangle" flags (triangles.cu); tri = 2 x the
 //     vertex's triangles, tri_deg = number of flagged edges (src/convert.cpp:271-340);
 //  4. triangle-free edges dropped and vertices ranked by (tri_deg, id)
 //     descending, degree-0 vertices trimmed (src/convert.cpp:342-414);
-//  5. the final symmetric CSR by a second key sort (src/convert.cpp:417-455).
+//  5. the final symmetric CSR: rows of the kept edges in rank ids, placed by
+//     the known row lengths (tri_deg) and sorted row by row (src/convert.cpp:417-455).
 #include "engine.cuh"
 
 namespace scd {
@@ -55,53 +56,51 @@ __global__ void k_rename(uint32_t *first, uint32_t n_raw, const uint32_t *__rest
     }
 }
 
-__global__ void k_directed_keys(const uint32_t *__restrict__ pairs, uint64_t count,
-                                const uint32_t *__restrict__ rename, int k, uint64_t *keys) {
-    const uint64_t sentinel = ~0ull >> (64 - 2 * k);
+// row lengths of the renamed, loop-free pairs in both directions
+__global__ void k_pair_degrees(const uint32_t *__restrict__ pairs, uint64_t count, const uint32_t *__restrict__ rename,
+                               uint32_t *cnt) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t a = rename[pairs[2 * i]], b = rename[pairs[2 * i + 1]];
-        if (a != b) {
-            keys[2 * i] = (a << k) | b;
-            keys[2 * i + 1] = (b << k) | a;
-        } else {
-            keys[2 * i] = sentinel;
-            keys[2 * i + 1] = sentinel;
+        const uint32_t a = rename[pairs[2 * i]], b = rename[pairs[2 * i + 1]];
+        if (a != b) {   // (input lists are often sorted by the first id: aggregate its increments)
+            warp_atomic_inc(cnt + a, __activemask());
+            atomicAdd(cnt + b, 1u);
         }
     }
 }
 
-struct FirstOfRun {
-    const uint64_t *keys;
-    uint64_t sentinel;
-    __device__ uint32_t operator[](size_t i) const {
-        uint64_t k = keys[i];
-        return k != sentinel && (i == 0 || keys[i - 1] != k);
+// both directions of every pair into their rows (order inside a row is fixed by the row sort)
+__global__ void k_pair_fill(const uint32_t *__restrict__ pairs, uint64_t count, const uint32_t *__restrict__ rename,
+                            const uint32_t *__restrict__ off, uint32_t *fill, uint32_t *vals) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = rename[pairs[2 * i]], b = rename[pairs[2 * i + 1]];
+        if (a != b) {
+            vals[off[a] + warp_atomic_inc(fill + a, __activemask())] = b;
+            vals[off[b] + atomicAdd(fill + b, 1u)] = a;
+        }
     }
+}
+
+struct NotInvalid {
+    const uint32_t *v;
+    __device__ uint32_t operator[](size_t i) const { return v[i] != INVALID; }
 };
 
-__global__ void k_compact_keys(const uint64_t *__restrict__ keys, uint64_t count, uint64_t sentinel,
-                               const uint32_t *__restrict__ pos, int k, uint32_t *rows, uint32_t *cols) {
-    const uint64_t mask = (1ull << k) - 1;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t key = keys[i];
-        if (key != sentinel && (i == 0 || keys[i - 1] != key)) {
-            uint32_t o = pos[i];
-            rows[o] = (uint32_t)(key >> k);
-            cols[o] = (uint32_t)(key & mask);
-        }
+__global__ void k_compact_vals(const uint32_t *__restrict__ vals, uint32_t count, const uint32_t *__restrict__ pos,
+                               uint32_t *out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t v = vals[i];
+        if (v != INVALID) out[pos[i]] = v;
     }
 }
 
-// row offsets of a row-sorted COO list: indices[r] = first slot of row >= r
-__global__ void k_row_offsets(const uint32_t *__restrict__ rows, uint32_t count, uint32_t n_rows,
-                              uint32_t *indices) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= count; i += gridDim.x * blockDim.x) {
-        uint32_t hi = i < count ? rows[i] : n_rows;
-        int64_t lo = i == 0 ? -1 : (int64_t)rows[i - 1];
-        for (int64_t r = lo + 1; r <= (int64_t)hi && r <= (int64_t)n_rows; r++) indices[r] = i;
-    }
+// rows[t] = r for every slot t of row r
+__global__ void k_fill_rows(const uint32_t *__restrict__ ind, uint32_t nrows, uint32_t *rows) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows; r += warps)
+        for (uint32_t t = ind[r] + lane; t < ind[r + 1]; t += 32) rows[t] = r;
 }
 
 struct IsOut {
@@ -177,37 +176,23 @@ __global__ void k_rank_of(const uint32_t *__restrict__ order, uint32_t n, const 
     }
 }
 
-struct Flagged {
-    const uint8_t *flag;
-    __device__ uint32_t operator[](size_t i) const { return flag[i] != 0; }
-};
-
-struct NonZeroDeg {
-    const int32_t *d;
-    __device__ uint32_t operator[](size_t i) const { return d[i] > 0; }
-};
-
-__global__ void k_final_keys(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
-                             const uint8_t *__restrict__ flag, const uint32_t *__restrict__ pos,
-                             uint32_t count, const uint32_t *__restrict__ rank, int k, uint64_t *keys) {
+// the kept (flagged) edges in rank ids into the rows of the final CSR, both directions
+__global__ void k_final_fill(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
+                             const uint8_t *__restrict__ flag, uint32_t count, const uint32_t *__restrict__ rank,
+                             const uint32_t *__restrict__ ind, uint32_t *fill, uint32_t *adj) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         if (flag[i]) {
-            uint64_t a = rank[orow[i]], b = rank[ocol[i]];
-            uint32_t o = pos[i];
-            keys[2 * (uint64_t)o] = (a << k) | b;
-            keys[2 * (uint64_t)o + 1] = (b << k) | a;
+            const uint32_t a = rank[orow[i]], b = rank[ocol[i]];
+            adj[ind[a] + warp_atomic_inc(fill + a, __activemask())] = b;
+            adj[ind[b] + atomicAdd(fill + b, 1u)] = a;
         }
     }
 }
 
-__global__ void k_split_keys(const uint64_t *__restrict__ keys, uint32_t count, int k, uint32_t *rows,
-                             uint32_t *cols) {
-    const uint64_t mask = (1ull << k) - 1;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        rows[i] = (uint32_t)(keys[i] >> k);
-        cols[i] = (uint32_t)(keys[i] & mask);
-    }
-}
+struct DegreeOf {   // final row length of a ranked vertex: its kept (triangle) edges
+    const int32_t *tri_deg;
+    __device__ uint32_t operator[](size_t i) const { return (uint32_t)tri_deg[i]; }
+};
 
 // ---- batches: graph g's records are [rec_off[g], rec_off[g+1]) --------------
 
@@ -409,25 +394,36 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
         CK(cudaMemcpyAsync(ren_off.get(), h, 8, cudaMemcpyHostToDevice, s));
     }
 
-    // 2. de-duplicated symmetric CSR over the renamed ids
+    // 2. de-duplicated symmetric CSR over the renamed ids: rows by a counting sort, then sorted row by row
     const int k1 = ceil_log2(n1 < 2 ? 2 : n1);
-    const uint64_t sent1 = ~0ull >> (64 - 2 * k1);
-    DevBuf<uint64_t> keys(2 * count, s);
-    k_directed_keys<<<G, TPB, 0, s>>>(pairs, count, rename.get(), k1, keys.get());
-    CK_LAUNCH("k_directed_keys");
+    DevBuf<uint32_t> cnt(n1, s), off1((size_t)n1 + 1, s);
+    CK(cudaMemsetAsync(cnt.get(), 0, (size_t)n1 * 4, s));
+    k_pair_degrees<<<G, TPB, 0, s>>>(pairs, count, rename.get(), cnt.get());
+    CK_LAUNCH("k_pair_degrees");
+    scan_exclusive<uint32_t>((const uint32_t *)cnt.get(), off1.get(), n1, s);
+    const uint32_t entries = read_scalar(off1.get() + n1, s);
+    DevBuf<uint32_t> vals(entries ? entries : 1, s);
+    CK(cudaMemsetAsync(cnt.get(), 0, (size_t)n1 * 4, s));
+    k_pair_fill<<<G, TPB, 0, s>>>(pairs, count, rename.get(), off1.get(), cnt.get(), vals.get());
+    CK_LAUNCH("k_pair_fill");
     rename.release();
-    radix_sort<uint64_t>(keys.get(), nullptr, 2 * count, 0, 2 * k1, s);
-    DevBuf<uint32_t> kpos(2 * count + 1, s);
-    scan_exclusive<uint32_t>(FirstOfRun{keys.get(), sent1}, kpos.get(), 2 * count, s);
-    const uint32_t slots1 = read_scalar(kpos.get() + 2 * count, s);
-    DevBuf<uint32_t> rows1(slots1, s), cols1(slots1, s), ind1(n1 + 1, s);
-    k_compact_keys<<<grid_for(2 * count, TPB), TPB, 0, s>>>(keys.get(), 2 * count, sent1, kpos.get(), k1,
-                                                           rows1.get(), cols1.get());
-    CK_LAUNCH("k_compact_keys");
-    keys.release();
-    kpos.release();
-    k_row_offsets<<<grid_for(slots1 + 1, TPB), TPB, 0, s>>>(rows1.get(), slots1, n1, ind1.get());
-    CK_LAUNCH("k_row_offsets");
+    sort_rows(c, off1.get(), n1, vals.get(), true, cnt.get(), s);   // cnt := distinct values of each row
+    DevBuf<uint32_t> ind1((size_t)n1 + 1, s);
+    scan_exclusive<uint32_t>((const uint32_t *)cnt.get(), ind1.get(), n1, s);
+    const uint32_t slots1 = read_scalar(ind1.get() + n1, s);
+    DevBuf<uint32_t> rows1(slots1 ? slots1 : 1, s), cols1(slots1 ? slots1 : 1, s);
+    {
+        DevBuf<uint32_t> vpos((size_t)entries + 1, s);
+        scan_exclusive<uint32_t>(NotInvalid{vals.get()}, vpos.get(), entries, s);
+        k_compact_vals<<<grid_for(entries, TPB), TPB, 0, s>>>(vals.get(), entries, vpos.get(), cols1.get());
+        CK_LAUNCH("k_compact_vals");
+    }
+    vals.release();
+    off1.release();
+    cnt.release();
+    k_fill_rows<<<grid_for((uint64_t)n1 * 32, TPB), TPB, 0, s>>>(ind1.get(), n1, rows1.get());
+    CK_LAUNCH("k_fill_rows");
+    c.launches += 5;
     const uint32_t m1 = slots1 / 2;
 
     // 3. degree orientation + triangle counts
@@ -479,21 +475,19 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     scan_exclusive<uint32_t>(KeptAt{order.get(), tdeg1.get()}, kscan.get(), n1, s);
     const uint32_t n2 = read_scalar(kscan.get() + n1, s);
 
-    // 5. final symmetric CSR in rank ids
-    DevBuf<uint32_t> fpos(m1 + 1, s);
-    scan_exclusive<uint32_t>(Flagged{oflag.get()}, fpos.get(), m1, s);
-    const uint32_t m2 = read_scalar(fpos.get() + m1, s);
-
+    // 5. final symmetric CSR in rank ids: row lengths are the kept edges (tri_deg), rows filled then sorted
     Graph &g = c.g;
     g.n = n2;
-    g.m = m2;
     g.indices = c.alloc<uint32_t>((size_t)n2 + 1);
-    g.adj = c.alloc<uint32_t>(2 * (size_t)m2);
     g.tri = c.alloc<int32_t>(n2);
     g.tri_deg = c.alloc<int32_t>(n2);
     k_rank_of<<<grid_for(n1, TPB), TPB, 0, s>>>(order.get(), n1, tri1.get(), tdeg1.get(), kscan.get(), rank.get(),
                                                g.tri, g.tri_deg);
     CK_LAUNCH("k_rank_of");
+    scan_exclusive<uint32_t>(DegreeOf{g.tri_deg}, g.indices, n2, s);
+    const uint32_t m2 = read_scalar(g.indices + n2, s) / 2;
+    g.m = m2;
+    g.adj = c.alloc<uint32_t>(2 * (size_t)m2);
     c.b.G = NG;
     c.b.fin_off = c.alloc<uint32_t>(NG + 1);
     k_final_offsets<<<grid_for(NG + 1, TPB), TPB, 0, s>>>(NG, ren_off.get(), kscan.get(), c.b.fin_off);
@@ -501,19 +495,13 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     c.b.h_fin_off.resize(NG + 1);
     CK(cudaMemcpyAsync(c.b.h_fin_off.data(), c.b.fin_off, 4 * (NG + 1), cudaMemcpyDeviceToHost, s));
     if (m2 > 0) {
-        const int k2 = ceil_log2(n2 < 2 ? 2 : n2);
-        DevBuf<uint64_t> fkeys(2 * (size_t)m2, s);
-        k_final_keys<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), oflag.get(), fpos.get(), m1,
-                                                      rank.get(), k2, fkeys.get());
-        CK_LAUNCH("k_final_keys");
-        radix_sort<uint64_t>(fkeys.get(), nullptr, 2 * (size_t)m2, 0, 2 * k2, s);
-        DevBuf<uint32_t> frows(2 * (size_t)m2, s);
-        k_split_keys<<<grid_for(2 * (size_t)m2, TPB), TPB, 0, s>>>(fkeys.get(), 2 * m2, k2, frows.get(), g.adj);
-        CK_LAUNCH("k_split_keys");
-        k_row_offsets<<<grid_for(2 * (size_t)m2 + 1, TPB), TPB, 0, s>>>(frows.get(), 2 * m2, n2, g.indices);
-        CK_LAUNCH("k_row_offsets");
-    } else {
-        CK(cudaMemsetAsync(g.indices, 0, ((size_t)n2 + 1) * 4, s));
+        DevBuf<uint32_t> fill(n2, s);
+        CK(cudaMemsetAsync(fill.get(), 0, (size_t)n2 * 4, s));
+        k_final_fill<<<grid_for(m1, TPB), TPB, 0, s>>>(orow.get(), ocol.get(), oflag.get(), m1, rank.get(), g.indices,
+                                                      fill.get(), g.adj);
+        CK_LAUNCH("k_final_fill");
+        sort_rows(c, g.indices, n2, g.adj, false, nullptr, s);
+        c.launches++;
     }
     c.has_graph = true;
     finish_graph(c);
