@@ -62,7 +62,9 @@ __global__ void k_bucket_scatter(uint32_t n, InBucket f, const uint32_t *__restr
 // and taken G at a time, the owner b of an item and the position of c in
 // out(a) are both found by binary search over registers (shuffles).  Per-slot
 // hit counts go to a 32-entry shared array per warp: a hit adds one for b and
-// one for c, both entries of out(a), and flags the (b, c) slot.
+// one for c, both entries of out(a), and flags the (b, c) slot.  An out(b) at
+// least 4x longer than out(a) (a hub's) is not walked: every lane searches its
+// out(a) entry in out(b) instead (alen searches of log2 d+(b) steps).
 template <int G>
 __global__ void __launch_bounds__(256)
 k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, LabelFilter lf, uint32_t *tcount,
@@ -71,6 +73,7 @@ k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, Labe
     __shared__ uint32_t acc[8][32];
     const uint32_t *labels = lf.labels;
     const int lane = threadIdx.x & 31, gl = lane % G, g0 = lane - gl, w = threadIdx.x >> 5;
+    const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << g0);
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * PER_WARP; base < nverts;
          base += warps * PER_WARP) {
@@ -86,7 +89,10 @@ k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, Labe
         const bool in_a = (uint32_t)gl < alen;
         const uint32_t x = in_a ? o.adj[abeg + gl] : 0xffffffffu;
         const bool ok = in_a && (!labels || labels[x] == la);   // usable as b and as c
-        const uint32_t wb = ok ? o.len[x] : 0u, bb = ok ? o.beg[x] : 0u;
+        const uint32_t wfull = ok ? o.len[x] : 0u, bb = ok ? o.beg[x] : 0u;
+        // a long out(b) is searched for the entries of out(a) (below) instead of walked
+        const bool far = wfull >= 32 && wfull >= 4 * alen;
+        const uint32_t wb = far ? 0u : wfull;
         uint32_t incl = wb;
 #pragma unroll
         for (int d = 1; d < G; d <<= 1) {
@@ -124,8 +130,39 @@ k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, Labe
                 hits++;
             }
         }
+        // long out-lists: lane k binary-searches its out(a) entry in out(b), one b at a time
         __syncwarp();
-        const uint32_t hc = acc[w][lane];
+        uint32_t selfc = 0;
+        // positions j that hold a far b in some group of the warp (groups search side by side)
+        const unsigned fm = __ballot_sync(FULL, far);
+        unsigned fpos = 0;
+#pragma unroll
+        for (int g = 0; g < PER_WARP; g++) fpos |= (G == 32) ? fm : (fm >> (g * G)) & ((1u << G) - 1u);
+        for (; fpos; fpos &= fpos - 1) {
+            const int j = __ffs(fpos) - 1;
+            const bool fj = __shfl_sync(FULL, far, j, G);
+            const uint32_t bj = __shfl_sync(FULL, bb, j, G), wj = __shfl_sync(FULL, wfull, j, G);
+            bool hit = false;
+            uint32_t lo = 0;
+            if (fj && ok) {
+                uint32_t hi = wj;
+                while (lo < hi) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (o.adj[bj + mid] < x) lo = mid + 1;
+                    else hi = mid;
+                }
+                hit = lo < wj && o.adj[bj + lo] == x;
+            }
+            if (hit) {
+                flag[bj + lo] = 1;
+                selfc++;
+                hits++;
+            }
+            const uint32_t nb = __popc(__ballot_sync(FULL, hit) & gmask);
+            if (gl == j && nb) acc[w][lane] += nb;
+        }
+        __syncwarp();
+        const uint32_t hc = acc[w][lane] + selfc;
         if (hc && in_a) {
             atomicAdd(tcount + x, hc);
             flag[abeg + gl] = 1;
@@ -226,6 +263,9 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
                     cv[k] = o.adj[cpos[k]];
                 }
             }
+            // a lane's items are in increasing order, so their owners b are too: hits of one
+            // b are summed in a register and added once (the b counter is shared by the warp)
+            uint32_t run_b = INVALID, run_hits = 0;
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
                 if (own[k] == INVALID) continue;
@@ -236,10 +276,16 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
                 while ((key = keys[w][h]) != c && key != EMPTY) h = (h + 1) & tmask;
                 if (key == c) {
                     atomicAdd(&cnt[w][idxs[w][h]], 1u);
-                    atomicAdd(&bhits[w][own[k]], 1u);
+                    if (own[k] != run_b) {
+                        if (run_hits) atomicAdd(&bhits[w][run_b], run_hits);
+                        run_b = own[k];
+                        run_hits = 0;
+                    }
+                    run_hits++;
                     flag[cpos[k]] = 1;
                 }
             }
+            if (run_hits) atomicAdd(&bhits[w][run_b], run_hits);
         }
         __syncwarp();
         const uint32_t hb = j < alen ? bhits[w][lane] : 0;
@@ -367,6 +413,9 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
                     cv[k] = o.adj[cpos[k]];
                 }
             }
+            // a lane's items are in increasing order, so their owners b are too: hits of one
+            // b are summed in a register and added once (the b counter is shared by the warp)
+            uint32_t run_b = INVALID, run_hits = 0;
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
                 if (own[k] == INVALID) continue;
@@ -377,10 +426,16 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
                 while ((key = keys[h]) != c && key != EMPTY) h = (h + 1) & tmask;
                 if (key == c) {
                     atomicAdd(&cnt[idxs[h]], 1u);
-                    atomicAdd(&bhits[own[k]], 1u);
+                    if (own[k] != run_b) {
+                        if (run_hits) atomicAdd(&bhits[run_b], run_hits);
+                        run_b = own[k];
+                        run_hits = 0;
+                    }
+                    run_hits++;
                     flag[cpos[k]] = 1;
                 }
             }
+            if (run_hits) atomicAdd(&bhits[run_b], run_hits);
         }
         __syncthreads();
         const uint32_t hb = j < alen ? bhits[threadIdx.x] : 0;
