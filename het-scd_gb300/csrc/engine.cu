@@ -215,6 +215,9 @@ PhaseScope::~PhaseScope() {
 
 void Ctx::free_all() {
     if (stream) cudaStreamSynchronize(stream);
+    if (side) cudaStreamSynchronize(side);
+    pext_join_pending = false;
+    pext_host_valid = false;
     for (void *p : owned) cudaFree(p);
     owned.clear();
     bytes = 0;
@@ -400,6 +403,7 @@ void set_labels(Ctx &c, const uint32_t *host_labels) {
 
 double iterate(Ctx &c) {
     // improve (old labels -> labels_next), statistics and WCC of the new labels
+    join_p_ext(c);
     improve(c, c.labels, c.st[c.cur], c.labels_next);
     uint32_t *t = c.labels;
     c.labels = c.labels_next;
@@ -479,6 +483,7 @@ void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int ma
     const double t0 = now_ms();
     if (!c.has_labels) initial_partition(c);
     launch_wcc(c, c.labels, c.st[c.cur]);
+    join_p_ext(c);   // p_ext (side stream) is needed from the first improvement on
     batch_reset(c);
     out.wcc0.resize(b.G);
     CK(cudaMemcpyAsync(out.wcc0.data(), b.wcc, 8 * b.G, cudaMemcpyDeviceToHost, s));
@@ -600,6 +605,7 @@ void scd_destroy(scd_ctx *ctx) {
     if (c.wcc_host) cudaFreeHost(c.wcc_host);
     if (c.host_u32) cudaFreeHost(c.host_u32);
     c.timers.destroy();
+    if (c.pext_ready) cudaEventDestroy(c.pext_ready);
     if (c.stream) cudaStreamDestroy(c.stream);
     if (c.side) cudaStreamDestroy(c.side);
     delete ctx;
@@ -637,7 +643,10 @@ int scd_graph_info(scd_ctx *ctx, uint32_t *n, uint32_t *m, double *cc) {
         require_graph(c);
         if (n) *n = c.g.n;
         if (m) *m = c.g.m;
-        if (cc) *cc = c.g.p_ext;
+        if (cc) {
+            host_p_ext(c);
+            *cc = c.g.p_ext;
+        }
     });
 }
 
@@ -810,7 +819,10 @@ int scd_batch_graph_info(scd_ctx *ctx, uint32_t g, uint32_t *n, uint32_t *m, dou
         if (g >= c.b.G) throw Error(SCD_ERR_ARG, "graph index out of range");
         if (n) *n = c.b.h_fin_off[g + 1] - c.b.h_fin_off[g];
         if (m) *m = c.b.h_m[g];
-        if (cc) *cc = c.b.h_p_ext[g];
+        if (cc) {
+            host_p_ext(c);
+            *cc = c.b.h_p_ext[g];
+        }
     });
 }
 

@@ -167,6 +167,9 @@ struct Ctx {
     Batch b;
     bool has_graph = false;
     bool capturing = false;           // inside a CUDA-graph capture: no host syncs, no timers
+    cudaEvent_t pext_ready = nullptr;  // p_ext (side stream) done
+    bool pext_join_pending = false;    // the main stream has not waited for it yet
+    bool pext_host_valid = false;      // b.h_p_ext / g.p_ext hold it
 
     // partition state
     uint32_t *labels = nullptr, *labels_next = nullptr, *best = nullptr;
@@ -220,7 +223,9 @@ double compute_wcc(Ctx &c, const uint32_t *labels, const Stats &st);
 void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bool frozen_graphs = false);
 // per-graph WCC in c.b.wcc (device); frozen_graphs: skip the graphs of a batch that stopped iterating
 void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_graphs = false);
-void compute_p_ext(Ctx &c);
+void compute_p_ext(Ctx &c);   // launches on the side stream
+void join_p_ext(Ctx &c);      // main stream waits for p_ext (outside captures)
+void host_p_ext(Ctx &c);      // host copies of p_ext (b.h_p_ext, g.p_ext)
 // per-graph loop control after a WCC (src/main.cpp:68-81): iteration count,
 // best WCC, best labels, convergence; *n_active receives the graphs still running
 void batch_step(Ctx &c, double threshold, double *trace = nullptr, int max_trace = 0);

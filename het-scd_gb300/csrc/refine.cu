@@ -5,9 +5,6 @@
 // wcc: internal triangles per edge by the oriented counting kernel restricted
 // to same-label triangles, per-vertex sums, per-vertex WCC terms and a
 // fixed-order (deterministic) tree reduction.
-#include <cmath>
-#include <vector>
-
 #include "engine.cuh"
 #include "gain.cuh"
 
@@ -464,10 +461,22 @@ double compute_wcc(Ctx &c, const uint32_t *labels, const Stats &st) {
     return *c.wcc_host;
 }
 
+// FP32 enclosure of every p_ext (directed conversions), for the interval gains
+__global__ void k_pe32(uint32_t G, const double *__restrict__ p_ext, float2 *pe32) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x)
+        pe32[g] = make_float2(__double2float_rd(p_ext[g]), __double2float_ru(p_ext[g]));
+}
+
+// p_ext of every graph on the side stream: the index-ordered sum is one CTA per
+// graph and runs alongside the initial partition and WCC on the main stream;
+// join_p_ext (before the first improvement) and host_p_ext (host reads) wait for it.
 void compute_p_ext(Ctx &c) {
     Graph &g = c.g;
     Batch &b = c.b;
-    cudaStream_t s = c.stream;
+    cudaStream_t s = c.side;
+    if (!c.pext_ready) CK(cudaEventCreateWithFlags(&c.pext_ready, cudaEventDisableTiming));
+    CK(cudaEventRecord(c.pext_ready, c.stream));   // the graph arrays are ready
+    CK(cudaStreamWaitEvent(s, c.pext_ready, 0));
     DevBuf<double> term(g.n ? g.n : 1, s);
     if (g.n) {
         k_pext_terms<<<grid_for(g.n, TPB), TPB, 0, s>>>(g.n, g.indices, g.tri, term.get());
@@ -489,20 +498,29 @@ void compute_p_ext(Ctx &c) {
         CK_LAUNCH("k_sequential_sum_exact");
         c.launches++;
     }
-    b.h_p_ext.resize(b.G);
-    CK(cudaMemcpyAsync(b.h_p_ext.data(), b.p_ext, sizeof(double) * b.G, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    g.p_ext = b.h_p_ext[0];
-    // FP32 enclosure of every p_ext for the interval gains
-    std::vector<float2> pe(b.G);
-    for (uint32_t i = 0; i < b.G; i++) {
-        const double d = b.h_p_ext[i];
-        const float f = (float)d;
-        pe[i] = make_float2((double)f > d ? std::nextafter(f, -INFINITY) : f,
-                            (double)f < d ? std::nextafter(f, INFINITY) : f);
-    }
-    CK(cudaMemcpyAsync(b.pe32, pe.data(), sizeof(float2) * b.G, cudaMemcpyHostToDevice, s));
-    CK(cudaStreamSynchronize(s));
+    k_pe32<<<grid_for(b.G, TPB), TPB, 0, s>>>(b.G, b.p_ext, b.pe32);
+    CK_LAUNCH("k_pe32");
+    c.launches++;
+    term.release();
+    CK(cudaEventRecord(c.pext_ready, s));
+    c.pext_join_pending = true;
+    c.pext_host_valid = false;
+}
+
+void join_p_ext(Ctx &c) {
+    if (!c.pext_join_pending) return;
+    CK(cudaStreamWaitEvent(c.stream, c.pext_ready, 0));
+    c.pext_join_pending = false;
+}
+
+void host_p_ext(Ctx &c) {
+    if (c.pext_host_valid) return;
+    Batch &b = c.b;
+    b.h_p_ext.assign(b.G, 0.0);
+    if (c.pext_ready) CK(cudaEventSynchronize(c.pext_ready));
+    if (b.G && b.p_ext) CK(cudaMemcpy(b.h_p_ext.data(), b.p_ext, sizeof(double) * b.G, cudaMemcpyDeviceToHost));
+    c.g.p_ext = b.G ? b.h_p_ext[0] : 0.0;
+    c.pext_host_valid = true;
 }
 
 }  // namespace scd

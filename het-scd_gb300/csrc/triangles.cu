@@ -263,9 +263,6 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
                     cv[k] = o.adj[cpos[k]];
                 }
             }
-            // a lane's items are in increasing order, so their owners b are too: hits of one
-            // b are summed in a register and added once (the b counter is shared by the warp)
-            uint32_t run_b = INVALID, run_hits = 0;
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
                 if (own[k] == INVALID) continue;
@@ -276,16 +273,10 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
                 while ((key = keys[w][h]) != c && key != EMPTY) h = (h + 1) & tmask;
                 if (key == c) {
                     atomicAdd(&cnt[w][idxs[w][h]], 1u);
-                    if (own[k] != run_b) {
-                        if (run_hits) atomicAdd(&bhits[w][run_b], run_hits);
-                        run_b = own[k];
-                        run_hits = 0;
-                    }
-                    run_hits++;
+                    atomicAdd(&bhits[w][own[k]], 1u);
                     flag[cpos[k]] = 1;
                 }
             }
-            if (run_hits) atomicAdd(&bhits[w][run_b], run_hits);
         }
         __syncwarp();
         const uint32_t hb = j < alen ? bhits[w][lane] : 0;
@@ -413,9 +404,6 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
                     cv[k] = o.adj[cpos[k]];
                 }
             }
-            // a lane's items are in increasing order, so their owners b are too: hits of one
-            // b are summed in a register and added once (the b counter is shared by the warp)
-            uint32_t run_b = INVALID, run_hits = 0;
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) {
                 if (own[k] == INVALID) continue;
@@ -426,16 +414,10 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
                 while ((key = keys[h]) != c && key != EMPTY) h = (h + 1) & tmask;
                 if (key == c) {
                     atomicAdd(&cnt[idxs[h]], 1u);
-                    if (own[k] != run_b) {
-                        if (run_hits) atomicAdd(&bhits[run_b], run_hits);
-                        run_b = own[k];
-                        run_hits = 0;
-                    }
-                    run_hits++;
+                    atomicAdd(&bhits[own[k]], 1u);
                     flag[cpos[k]] = 1;
                 }
             }
-            if (run_hits) atomicAdd(&bhits[run_b], run_hits);
         }
         __syncthreads();
         const uint32_t hb = j < alen ? bhits[threadIdx.x] : 0;
