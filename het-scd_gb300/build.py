@@ -19,8 +19,8 @@ ORACLE = os.path.join(ROOT, "oracle")
 REF_SRC = "/root/reference/src"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["engine.cu", "preprocess.cu", "csr.cu", "triangles.cu", "partition.cu", "refine.cu", "improve.cu",
-              "wcc_static.cu"]
+CU_SOURCES = ["engine.cu", "preprocess.cu", "csr.cu", "text.cu", "triangles.cu", "partition.cu", "refine.cu",
+              "improve.cu", "wcc_static.cu"]
 
 
 def _run(cmd, cwd=None):

@@ -765,6 +765,47 @@ int scd_run(scd_ctx *ctx, double threshold, int max_iters, double *wcc_trace, sc
     });
 }
 
+namespace {
+// the text in device memory (copied in if it is on the host)
+const char *device_text(Ctx &c, const char *text, uint64_t bytes, int on_device, DevBuf<char> &tmp) {
+    if (bytes && !text) throw Error(SCD_ERR_ARG, "text is NULL");
+    if (on_device || bytes == 0) return text;
+    tmp.alloc(bytes, c.stream);
+    CK(cudaMemcpyAsync(tmp.get(), text, bytes, cudaMemcpyHostToDevice, c.stream));
+    return tmp.get();
+}
+}  // namespace
+
+int scd_convert_text(scd_ctx *ctx, const char *text, uint64_t bytes, int text_on_device) {
+    return guarded(ctx, [&](Ctx &c) {
+        DevBuf<char> tmp;
+        const char *d = device_text(c, text, bytes, text_on_device, tmp);
+        DevBuf<uint32_t> pairs;
+        uint64_t count;
+        {
+            PhaseScope ph(c, "parse");
+            count = parse_edge_text(c, d, bytes, pairs);
+        }
+        tmp.release();
+        convert_edges(c, pairs.get(), count);
+        CK(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int scd_parse_text(scd_ctx *ctx, const char *text, uint64_t bytes, int text_on_device, uint32_t *pairs,
+                   uint64_t *count) {
+    return guarded(ctx, [&](Ctx &c) {
+        if (!count) throw Error(SCD_ERR_ARG, "count is NULL");
+        DevBuf<char> tmp;
+        const char *d = device_text(c, text, bytes, text_on_device, tmp);
+        DevBuf<uint32_t> out;
+        *count = parse_edge_text(c, d, bytes, out);
+        if (pairs && *count)
+            CK(cudaMemcpyAsync(pairs, out.get(), 8 * *count, cudaMemcpyDeviceToHost, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+    });
+}
+
 int scd_batch_convert(scd_ctx *ctx, const uint32_t *pairs, const uint64_t *record_offsets, uint32_t num_graphs,
                       int pairs_on_device) {
     return guarded(ctx, [&](Ctx &c) {

@@ -208,6 +208,8 @@ struct Ctx {
 // rec_off (host, G+1 entries, nullable): records of graph g are [rec_off[g], rec_off[g+1]),
 // each graph with its own vertex ids; the graphs become one block-diagonal union.
 void convert_edges(Ctx &c, const uint32_t *pairs_dev, uint64_t count, const std::vector<uint64_t> *rec_off = nullptr);
+// read_edges on the device: (min, max) records of the text in file order into out
+uint64_t parse_edge_text(Ctx &c, const char *text, uint64_t bytes, DevBuf<uint32_t> &out);
 void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
                   const int32_t *tri, const int32_t *tri_deg);
 void finish_graph(Ctx &c);   // nlow, p_ext, degree classes, partition buffers

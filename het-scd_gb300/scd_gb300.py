@@ -20,7 +20,7 @@ ERRORS = {-1: "SCD_ERR_ARG", -2: "SCD_ERR_CUDA", -3: "SCD_ERR_OOM", -4: "SCD_ERR
           -5: "SCD_ERR_FORMAT", -6: "SCD_ERR_TIMEOUT", -7: "SCD_ERR_LIMIT"}
 INVALID_LABEL = 0xFFFFFFFF
 FLAG_PROFILE, FLAG_PEXT_TREE, FLAG_NO_GRAPHS = 1, 2, 4
-PHASES = ("convert", "tc", "partition", "improve", "stats", "wcc_tc", "wcc")
+PHASES = ("parse", "convert", "tc", "partition", "improve", "stats", "wcc_tc", "wcc")
 
 
 class ScdError(RuntimeError):
@@ -78,6 +78,8 @@ def lib():
             "scd_batch_run": ([P, dbl, i32, P], i32),
             "scd_batch_labels": ([P, u32, P], i32),
             "scd_batch_convert_lists": ([P, P, P, u32], i32),
+            "scd_convert_text": ([P, ctypes.c_char_p, u64, i32], i32),
+            "scd_parse_text": ([P, ctypes.c_char_p, u64, i32, P, ctypes.POINTER(u64)], i32),
             "scd_batch_labels_all": ([P, P, P], i32),
             "scd_autotune": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(dbl),
                               ctypes.c_char_p, u64], i32),
@@ -139,6 +141,20 @@ class Engine:
             return
         pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1, 2)
         self._check(lib().scd_convert_edges(self._ctx, _p(pairs), pairs.shape[0], 0))
+
+    def convert_text(self, text):
+        """Device parse of an edge-list text (bytes) and device preprocessing."""
+        text = bytes(text)
+        self._check(lib().scd_convert_text(self._ctx, text, len(text), 0))
+
+    def parse_text(self, text):
+        """The (min, max) records of an edge-list text, parsed on the device."""
+        text = bytes(text)
+        cnt = ctypes.c_uint64()
+        self._check(lib().scd_parse_text(self._ctx, text, len(text), 0, None, ctypes.byref(cnt)))
+        out = np.empty((max(cnt.value, 1), 2), np.uint32)
+        self._check(lib().scd_parse_text(self._ctx, text, len(text), 0, _p(out), ctypes.byref(cnt)))
+        return out[: cnt.value]
 
     def transfer_graph(self, g, alpha=1.0):
         arrs = [np.ascontiguousarray(getattr(g, k), dtype=t) for k, t in

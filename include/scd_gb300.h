@@ -64,6 +64,20 @@ const char *scd_last_error(const scd_ctx *ctx);
  * pointer.  The resulting graph stays resident in the context. */
 int scd_convert_edges(scd_ctx *ctx, const uint32_t *pairs, uint64_t count, int pairs_on_device);
 
+/* Replaces read_edges (src/convert.cpp:74-138) followed by the processing of
+ * scd_convert_edges: the edge-list text (bytes characters; a device pointer if
+ * text_on_device) is parsed on the device with the reference's line rules
+ * ('\n'-separated lines of at most 1023 characters, leading blanks skipped,
+ * empty and '#' lines ignored, two unsigned decimal numbers, the record is
+ * (min, max)) and converted.  SCD_ERR_FORMAT with the reference's message for
+ * the first failing line ("line i is corrupt", or a line longer than 1023
+ * characters). */
+int scd_convert_text(scd_ctx *ctx, const char *text, uint64_t bytes, int text_on_device);
+/* The parse alone: *count receives the number of records and, if pairs (host)
+ * is not NULL, pairs receives them (2 * count words, file order). */
+int scd_parse_text(scd_ctx *ctx, const char *text, uint64_t bytes, int text_on_device, uint32_t *pairs,
+                   uint64_t *count);
+
 /* Replaces cuda_transfer_graph(const Graph*, alpha) (src/cuda.hpp:24,
  * src/cuda.cu:84-148): uploads a graph in the binary-format layout
  * (src/graph.cpp:86-134).  The clustering coefficient p_ext
