@@ -280,6 +280,9 @@ def bench_batched(S, device, args):
                         "mu U[0.05,0.4], seeds 4..",
             "graphs": k, "edges_in": records, "batches": len(groups), "max_records_per_batch": args.batch_records,
             "graphs_per_s": b_gps, "edges_per_s": records / batch_s, "seconds": batch_s,
+            "e2e_text": {"value": world * E / (text_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": len(text),
+                         "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1),
+                         "note": "from the edge-list text in host memory: device parse + preprocessing + SCD + labels"},
             "gpu_launches": launches, "peak_engine_bytes": mem, "not_converged_batches": not_converged,
             "per_graph_loop": {"graphs_per_s": l_gps, "edges_per_s": loop_records / loop_s, "sample_graphs": len(sample),
                                "seconds": loop_s},
@@ -473,6 +476,27 @@ def bench_plain(S, args, world, rank, local, dist):
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t) * 1e3 / args.steps
     n, m, cc = eng.graph_info()
+    # end to end from the edge-list TEXT in host memory (device parse, as read_edges + convert + main-gpu)
+    import tempfile
+    with tempfile.NamedTemporaryFile(suffix=".txt", delete=False) as f:
+        tpath = f.name
+    scdgen.write_text(tpath, pairs)
+    with open(tpath, "rb") as f:
+        text = f.read()
+    os.unlink(tpath)
+
+    def step_text():
+        eng.convert_text(text)
+        r = eng.run(0.01, 1000)
+        return r, eng.labels_from_device()
+
+    step_text()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step_text()
+    torch.cuda.synchronize()
+    text_ms = (time.perf_counter() - t) * 1e3 / args.steps
 
     if dist:
         tt = torch.tensor([dev_ms, e2e_ms], device="cuda")
@@ -517,6 +541,9 @@ def bench_plain(S, args, world, rank, local, dist):
                        "l2": "inputs larger than L2 (edge list %d MB)" % (E * 8 >> 20)},
             "e2e": {"value": world * E / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": E * 8,
                     "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1)},
+            "e2e_text": {"value": world * E / (text_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": len(text),
+                         "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1),
+                         "note": "from the edge-list text in host memory: device parse + preprocessing + SCD + labels"},
             "gpu_launches": launches,
             "phases_ms": {p: round(v[0], 3) for p, v in prof.items()},
             "roofline": {"kernel": "k_tc_warp + k_tc_cta (preprocessing triangle counting)", "bound": "hbm",
