@@ -4,8 +4,9 @@
 // Instead of one global sort of 64-bit (row, value) keys, whose every radix
 // pass moves every entry, the entries are placed by a counting sort on the row
 // (row lengths, offsets, one scatter) and then every row is sorted on its own:
-//   rows of length <= 32      a warp, bitonic network in registers;
-//   33 .. 512, 513 .. 4096    a CTA, bitonic network in shared memory;
+//   rows of length <= 128     a warp, bitonic network in registers (1, 2 or 4
+//                             values per lane);
+//   129 .. 512, 513 .. 4096   a CTA, bitonic network in shared memory;
 //   longer rows               one radix sort of (row rank, value) keys.
 // With de-duplication a repeated value of a row becomes INVALID and the number
 // of distinct values of the row is written out; the caller compacts.
@@ -47,6 +48,65 @@ k_sort_rows_warp(const uint32_t *__restrict__ off, uint32_t nrows, uint32_t *val
         if (in) vals[beg + lane] = keep ? v : INVALID;
         const unsigned kb = __ballot_sync(FULL, keep);
         if (udeg && lane == 0) udeg[r] = __popc(kb);
+    }
+}
+
+// rows of one list with 32 < len <= 32 * E: one warp per row, E values per lane
+// (value index = lane * E + i), bitonic network in registers
+template <int E>
+__global__ void __launch_bounds__(TPB)
+k_sort_rows_warp_e(const uint32_t *__restrict__ list, uint32_t count, const uint32_t *__restrict__ off, uint32_t *vals,
+                   bool dedup, uint32_t *udeg) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < count; w += warps) {
+        const uint32_t r = list[w], beg = off[r], len = off[r + 1] - beg;
+        uint32_t v[E];
+#pragma unroll
+        for (int i = 0; i < E; i++) {
+            const uint32_t idx = lane * E + i;
+            v[i] = idx < len ? vals[beg + idx] : INVALID;
+        }
+#pragma unroll
+        for (int k = 2; k <= 32 * E; k <<= 1) {
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                if (j >= E) {   // partner in lane ^ (j / E)
+#pragma unroll
+                    for (int i = 0; i < E; i++) {
+                        const int idx = lane * E + i;
+                        const uint32_t o = __shfl_xor_sync(FULL, v[i], j / E);
+                        const bool asc = (idx & k) == 0, low = (idx & j) == 0;
+                        v[i] = (low == asc) ? min(v[i], o) : max(v[i], o);
+                    }
+                } else {        // partner in this lane: i ^ j
+#pragma unroll
+                    for (int i = 0; i < E; i++) {
+                        const int q = i ^ j;
+                        if (q > i) {
+                            const bool asc = ((lane * E + i) & k) == 0;
+                            const uint32_t x = v[i], y = v[q];
+                            if ((x > y) == asc) {
+                                v[i] = y;
+                                v[q] = x;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        const uint32_t last_prev = __shfl_up_sync(FULL, v[E - 1], 1);
+        uint32_t kept = 0;
+#pragma unroll
+        for (int i = 0; i < E; i++) {
+            const uint32_t idx = lane * E + i;
+            const uint32_t prev = i ? v[i - 1] : last_prev;
+            const bool keep = idx < len && (!dedup || idx == 0 || v[i] != prev);
+            if (idx < len) vals[beg + idx] = keep ? v[i] : INVALID;
+            kept += keep;
+        }
+        kept = warp_sum(kept);
+        if (udeg && lane == 0) udeg[r] = kept;
     }
 }
 
@@ -154,18 +214,19 @@ void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool
     k_sort_rows_warp<<<grid_for((uint64_t)nrows * 32, TPB), TPB, 0, s>>>(off, nrows, vals, dedup, udeg);
     CK_LAUNCH("k_sort_rows_warp");
     c.launches++;
-    // the longer rows, listed by length class (one host read for the three counts)
-    const uint32_t bounds[4] = {WARP_ROW, MID_ROW, BIG_ROW, 0xffffffffu};
-    DevBuf<uint32_t> pos[3];
-    for (int k = 0; k < 3; k++) {
+    // the longer rows, listed by length class (one host read for all the counts)
+    constexpr int NC = 5;
+    const uint32_t bounds[NC + 1] = {WARP_ROW, 64, 128, MID_ROW, BIG_ROW, 0xffffffffu};
+    DevBuf<uint32_t> pos[NC];
+    for (int k = 0; k < NC; k++) {
         pos[k].alloc((size_t)nrows + 1, s);
         scan_exclusive<uint32_t>(RowLenIn{off, bounds[k], bounds[k + 1]}, pos[k].get(), nrows, s);
     }
-    uint32_t cnt[3];
-    for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(cnt + k, pos[k].get() + nrows, 4, cudaMemcpyDeviceToHost, s));
+    uint32_t cnt[NC];
+    for (int k = 0; k < NC; k++) CK(cudaMemcpyAsync(cnt + k, pos[k].get() + nrows, 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    DevBuf<uint32_t> list[3];
-    for (int k = 0; k < 3; k++) {
+    DevBuf<uint32_t> list[NC];
+    for (int k = 0; k < NC; k++) {
         if (!cnt[k]) continue;
         list[k].alloc(cnt[k], s);
         k_row_scatter<<<grid_for(nrows, TPB), TPB, 0, s>>>(nrows, RowLenIn{off, bounds[k], bounds[k + 1]},
@@ -174,33 +235,45 @@ void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool
         c.launches++;
     }
     if (cnt[0]) {
-        k_sort_rows_cta<128, MID_ROW><<<grid_for(cnt[0], 1, 152 * 16), 128, 0, s>>>(list[0].get(), cnt[0], off, vals,
+        k_sort_rows_warp_e<2><<<grid_for((uint64_t)cnt[0] * 32, TPB), TPB, 0, s>>>(list[0].get(), cnt[0], off, vals,
+                                                                                dedup, udeg);
+        CK_LAUNCH("k_sort_rows_warp64");
+        c.launches++;
+    }
+    if (cnt[1]) {
+        k_sort_rows_warp_e<4><<<grid_for((uint64_t)cnt[1] * 32, TPB), TPB, 0, s>>>(list[1].get(), cnt[1], off, vals,
+                                                                                dedup, udeg);
+        CK_LAUNCH("k_sort_rows_warp128");
+        c.launches++;
+    }
+    if (cnt[2]) {
+        k_sort_rows_cta<128, MID_ROW><<<grid_for(cnt[2], 1, 152 * 16), 128, 0, s>>>(list[2].get(), cnt[2], off, vals,
                                                                                  dedup, udeg);
         CK_LAUNCH("k_sort_rows_cta512");
         c.launches++;
     }
-    if (cnt[1]) {
-        k_sort_rows_cta<512, BIG_ROW><<<grid_for(cnt[1], 1, 152 * 4), 512, 0, s>>>(list[1].get(), cnt[1], off, vals,
+    if (cnt[3]) {
+        k_sort_rows_cta<512, BIG_ROW><<<grid_for(cnt[3], 1, 152 * 4), 512, 0, s>>>(list[3].get(), cnt[3], off, vals,
                                                                                 dedup, udeg);
         CK_LAUNCH("k_sort_rows_cta4096");
         c.launches++;
     }
-    if (cnt[2]) {
-        DevBuf<uint32_t> koff((size_t)cnt[2] + 1, s);
-        scan_exclusive<uint32_t>(RowLenOf{list[2].get(), off}, koff.get(), cnt[2], s);
+    if (cnt[4]) {
+        DevBuf<uint32_t> koff((size_t)cnt[4] + 1, s);
+        scan_exclusive<uint32_t>(RowLenOf{list[4].get(), off}, koff.get(), cnt[4], s);
         uint32_t total = 0;
-        CK(cudaMemcpyAsync(&total, koff.get() + cnt[2], 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&total, koff.get() + cnt[4], 4, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         DevBuf<uint64_t> keys(total, s);
-        k_big_keys<<<grid_for(cnt[2], 1, 152 * 8), TPB, 0, s>>>(list[2].get(), cnt[2], off, koff.get(), vals,
+        k_big_keys<<<grid_for(cnt[4], 1, 152 * 8), TPB, 0, s>>>(list[4].get(), cnt[4], off, koff.get(), vals,
                                                                keys.get());
         CK_LAUNCH("k_big_keys");
-        radix_sort<uint64_t>(keys.get(), nullptr, total, 0, 32 + ceil_log2(cnt[2] < 2 ? 2 : cnt[2]), s);
+        radix_sort<uint64_t>(keys.get(), nullptr, total, 0, 32 + ceil_log2(cnt[4] < 2 ? 2 : cnt[4]), s);
         if (udeg) {
-            k_zero_rows<<<grid_for(cnt[2], TPB), TPB, 0, s>>>(list[2].get(), cnt[2], udeg);
+            k_zero_rows<<<grid_for(cnt[4], TPB), TPB, 0, s>>>(list[4].get(), cnt[4], udeg);
             CK_LAUNCH("k_zero_rows");
         }
-        k_big_back<<<grid_for(total, TPB), TPB, 0, s>>>(keys.get(), total, list[2].get(), off, koff.get(), vals,
+        k_big_back<<<grid_for(total, TPB), TPB, 0, s>>>(keys.get(), total, list[4].get(), off, koff.get(), vals,
                                                         dedup, udeg);
         CK_LAUNCH("k_big_back");
         c.launches += 3;
