@@ -218,7 +218,7 @@ void Ctx::free_all() {
     if (side) cudaStreamSynchronize(side);
     pext_join_pending = false;
     pext_host_valid = false;
-    for (void *p : owned) cudaFree(p);
+    for (void *p : owned) cudaFreeAsync(p, stream);
     owned.clear();
     bytes = 0;
     g = Graph();
@@ -583,6 +583,12 @@ int scd_create(scd_ctx **out, int device_id, int work_group_size, unsigned flags
     c.flags = flags;
     try {
         CK(cudaSetDevice(device_id));
+        {   // keep freed pool memory cached for the next graph instead of returning it at every sync
+            cudaMemPool_t pool;
+            CK(cudaDeviceGetDefaultMemPool(&pool, device_id));
+            uint64_t keep = ~0ull;
+            CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        }
         CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
         CK(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
         CK(cudaMalloc((void **)&c.work_counter, 64));
@@ -601,6 +607,11 @@ void scd_destroy(scd_ctx *ctx) {
     Ctx &c = ctx->c;
     cudaSetDevice(c.device);
     c.free_all();
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    {   // hand the cached pool memory back (arrays still in use elsewhere are not affected)
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, c.device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    }
     if (c.work_counter) cudaFree(c.work_counter);
     if (c.wcc_host) cudaFreeHost(c.wcc_host);
     if (c.host_u32) cudaFreeHost(c.host_u32);

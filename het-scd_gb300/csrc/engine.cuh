@@ -192,11 +192,14 @@ struct Ctx {
     std::vector<void *> owned;        // device allocations freed with the graph
     uint64_t bytes = 0;
 
+    // graph-lifetime device arrays: stream-ordered from the device's memory pool, which
+    // keeps freed memory cached (release threshold raised at scd_create), so a new graph
+    // reuses the previous one's memory without cudaMalloc/cudaFree synchronisation
     template <typename T>
     T *alloc(size_t count) {
         void *p = nullptr;
         if (count == 0) count = 1;
-        CK(cudaMalloc(&p, count * sizeof(T)));
+        CK(cudaMallocAsync(&p, count * sizeof(T), stream));
         owned.push_back(p);
         bytes += count * sizeof(T);
         return (T *)p;

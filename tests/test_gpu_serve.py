@@ -27,9 +27,10 @@ def test_results_identical_alone_and_in_the_mix():
     reqs_pairs = _requests(30, 5)
     with serve.Server(device=0, workers=3, max_batch=8) as srv:
         reqs = []
-        for p in reqs_pairs:
+        for i, p in enumerate(reqs_pairs):
             reqs.append(srv.submit(p))
-            time.sleep(0.002)   # arrivals while earlier batches run
+            if i >= 12:
+                time.sleep(0.002)   # after a burst (batched), arrivals while earlier batches run
         outs = [r.wait(120) for r in reqs]
         assert sum(b for b, _ in srv.batches) == len(reqs)
         assert max(b for b, _ in srv.batches) > 1   # batching happened
