@@ -280,9 +280,6 @@ def bench_batched(S, device, args):
                         "mu U[0.05,0.4], seeds 4..",
             "graphs": k, "edges_in": records, "batches": len(groups), "max_records_per_batch": args.batch_records,
             "graphs_per_s": b_gps, "edges_per_s": records / batch_s, "seconds": batch_s,
-            "e2e_text": {"value": world * E / (text_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": len(text),
-                         "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1),
-                         "note": "from the edge-list text in host memory: device parse + preprocessing + SCD + labels"},
             "gpu_launches": launches, "peak_engine_bytes": mem, "not_converged_batches": not_converged,
             "per_graph_loop": {"graphs_per_s": l_gps, "edges_per_s": loop_records / loop_s, "sample_graphs": len(sample),
                                "seconds": loop_s},
