@@ -160,8 +160,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": K, "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
-            "config": {"workload": f"rmat-{CPU_SAMPLE_SCALE} sample of rmat-22 (edge factor 16, a/b/c/d .57/.19/.19/.05)",
-                       "edges_in": e, "l2": "inputs larger than L2"},
+            "config": {"workload": f"rmat-{args.scale}", "edge_factor": 16, "abcd": [0.57, 0.19, 0.19, 0.05],
+                       "parallelism": f"host cores ({cores} threads)",
+                       "sample": f"each step: R-MAT scale {CPU_SAMPLE_SCALE} of the same generator ({e} edges)"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"R-MAT scale {CPU_SAMPLE_SCALE} (same generator and a,b,c,d), "
                                        "reference timers: process graph + initial partition + initial WCC + iterations"},
