@@ -41,6 +41,43 @@ __device__ __forceinline__ RowSeg chunk_seg(const RowWork &rw, uint32_t c, const
     return r;
 }
 
+// A warp takes 32 consecutive rows (lane k: row r0 + k, its entries [b_k, b_k + len_k))
+// and walks their concatenated entries 32 at a time: coalesced loads and many
+// independent gathers in flight instead of one short row per warp.  For the entry
+// of lane L the owning row is found by a binary search over the lanes' prefix
+// sums (shuffles); each lane then counts, with one ballot, the hits of its own
+// row in the chunk (the chunk lanes owned by row k form one contiguous range).
+struct RowStream {
+    uint32_t pre, len, total;
+    __device__ __forceinline__ RowStream(uint32_t l) : len(l) {
+        const int lane = threadIdx.x & 31;
+        uint32_t incl = l;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t y = __shfl_up_sync(FULL, incl, d);
+            if (lane >= d) incl += y;
+        }
+        total = __shfl_sync(FULL, incl, 31);
+        pre = incl - l;
+    }
+    // owner lane of stream position t (t < total)
+    __device__ __forceinline__ int owner(uint32_t t) const {
+        int j = 0;
+#pragma unroll
+        for (int st = 16; st > 0; st >>= 1)
+            if (__shfl_sync(FULL, pre, j + st) <= t) j += st;
+        return j;
+    }
+    // lanes of the chunk [t0, t0 + 32) that hold this lane's row
+    __device__ __forceinline__ unsigned my_lanes(uint32_t t0) const {
+        const long long lo = (long long)pre - t0, hi = (long long)pre + len - t0;
+        const int a = lo <= 0 ? 0 : lo >= 32 ? 32 : (int)lo, b = hi <= 0 ? 0 : hi >= 32 ? 32 : (int)hi;
+        const unsigned upto_b = b >= 32 ? FULL : ((1u << b) - 1u);
+        const unsigned upto_a = a >= 32 ? FULL : ((1u << a) - 1u);
+        return upto_b & ~upto_a;
+    }
+};
+
 // collect_stats for one row segment: sizes once per vertex, ext/int from the segment
 template <int G>
 __device__ __forceinline__ void stats_seg(RowSeg r, const uint32_t *adj, const uint32_t *labels, Stats st,
@@ -61,26 +98,43 @@ __device__ __forceinline__ void stats_seg(RowSeg r, const uint32_t *adj, const u
     }
 }
 
-// collect_stats (src/scd.cpp:57-111): one warp per vertex of degree <= 256 in id
-// order (short dependent-load chains, consecutive warps on consecutive rows),
-// the rows longer than 256 as RowWork chunks after them
+// collect_stats (src/scd.cpp:57-111): rows of degree <= 256 as 32-row streams in id
+// order, the rows longer than 256 as RowWork chunks after them
 __global__ void __launch_bounds__(TPB)
 k_stats(uint32_t n, RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
         const uint32_t *__restrict__ labels, Stats st, LabelFilter skip) {
+    const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nchunks = rw.nchunks;
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n + nchunks; w += warps) {
-        RowSeg r;
-        if (w < n) {
-            r.v = w;
-            r.row0 = r.beg = indices[w];
-            r.end = indices[w + 1];
-            r.first = true;
-            r.live = r.end - r.beg <= RowWork::CHUNK;
-        } else {
-            r = chunk_seg(rw, w - n, indices);
+    const uint32_t groups = (n + 31) / 32, nchunks = rw.nchunks;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < groups + nchunks; w += warps) {
+        if (w >= groups) {   // a piece of a long row
+            stats_seg<32>(chunk_seg(rw, w - groups, indices), adj, labels, st, skip);
+            continue;
         }
-        stats_seg<32>(r, adj, labels, st, skip);
+        const uint32_t r = w * 32 + lane;
+        uint32_t b = 0, deg = 0, l = INVALID;
+        if (r < n) {
+            b = indices[r];
+            deg = indices[r + 1] - b;
+            l = labels[r];
+            if (skip.frozen(r)) l = INVALID;
+        }
+        const bool mine = l != INVALID && deg <= RowWork::CHUNK;   // long rows: chunk units
+        const RowStream rs(mine ? deg : 0u);
+        uint32_t same = 0;
+        for (uint32_t t0 = 0; t0 < rs.total; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            const int j = rs.owner(t < rs.total ? t : rs.total - 1);
+            const uint32_t pos = __shfl_sync(FULL, b, j) + (t - __shfl_sync(FULL, rs.pre, j));
+            const uint32_t lj = __shfl_sync(FULL, l, j);
+            const bool hit = t < rs.total && labels[adj[pos]] == lj;
+            same += __popc(__ballot_sync(FULL, hit) & rs.my_lanes(t0));
+        }
+        if (mine) {
+            atomicAdd(st.sizes + l, 1);
+            if (deg - same) atomicAdd(st.ext + l, (int)(deg - same));
+            if (same) atomicAdd(st.intl + l, (int)same);
+        }
     }
 }
 
@@ -108,28 +162,37 @@ __device__ __forceinline__ void intdeg_seg(RowSeg r, const uint32_t *nlow, const
 }
 
 // int_tri_deg (src/wcc.cpp:124-126): per vertex, the internal edges that lie on an
-// internal triangle, counted from the out-slot flags of both endpoints
-// int_tri_deg (src/wcc.cpp:124-126): per vertex, the internal edges that lie on an
-// internal triangle, counted from the out-slot flags of both endpoints; one warp
-// per vertex of degree <= 256 in id order, longer rows as RowWork chunks
+// internal triangle, counted from the out-slot flags of both endpoints; the out-slots
+// of rows of degree <= 256 as 32-row streams in id order, longer rows as RowWork chunks
 __global__ void __launch_bounds__(TPB)
 k_internal_degrees(uint32_t n, RowWork rw, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
                    const uint32_t *__restrict__ adj, const uint8_t *__restrict__ flag, int32_t *itdeg,
                    LabelFilter skip) {
+    const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t nchunks = rw.nchunks;
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n + nchunks; w += warps) {
-        RowSeg r;
-        if (w < n) {
-            r.v = w;
-            r.row0 = r.beg = indices[w];
-            r.end = indices[w + 1];
-            r.first = true;
-            r.live = r.end - r.beg <= RowWork::CHUNK;
-        } else {
-            r = chunk_seg(rw, w - n, indices);
+    const uint32_t groups = (n + 31) / 32, nchunks = rw.nchunks;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < groups + nchunks; w += warps) {
+        if (w >= groups) {   // a piece of a long row
+            intdeg_seg<32>(chunk_seg(rw, w - groups, indices), nlow, adj, flag, itdeg, skip);
+            continue;
         }
-        intdeg_seg<32>(r, nlow, adj, flag, itdeg, skip);
+        const uint32_t u = w * 32 + lane;
+        uint32_t b = 0, len = 0;
+        if (u < n && !skip.frozen(u)) {
+            b = indices[u];
+            if (indices[u + 1] - b <= RowWork::CHUNK) len = nlow[u];
+        }
+        const RowStream rs(len);
+        uint32_t edges = 0;
+        for (uint32_t t0 = 0; t0 < rs.total; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            const int j = rs.owner(t < rs.total ? t : rs.total - 1);
+            const uint32_t pos = __shfl_sync(FULL, b, j) + (t - __shfl_sync(FULL, rs.pre, j));
+            const bool f = t < rs.total && flag[pos];
+            if (f) atomicAdd(itdeg + adj[pos], 1);
+            edges += __popc(__ballot_sync(FULL, f) & rs.my_lanes(t0));
+        }
+        if (edges) atomicAdd(itdeg + u, (int)edges);
     }
 }
 
@@ -419,8 +482,8 @@ void collect_stats(Ctx &c, const uint32_t *labels, Stats &st, bool frozen_graphs
     if (g.n == 0) return;
     PhaseScope ph(c, "stats");
     const LabelFilter skip{nullptr, c.b.gid, frozen_graphs ? c.b.active : nullptr};
-    k_stats<<<grid_for(((uint64_t)g.n + g.rows.nchunks) * 32, TPB), TPB, 0, s>>>(g.n, g.rows, g.indices,
-                                                                                          g.adj, labels, st, skip);
+    k_stats<<<grid_for(((uint64_t)(g.n + 31) / 32 + g.rows.nchunks) * 32, TPB), TPB, 0, s>>>(
+        g.n, g.rows, g.indices, g.adj, labels, st, skip);
     CK_LAUNCH("k_stats");
     c.launches++;
 }
@@ -441,7 +504,7 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_gra
     const uint8_t *active = frozen_graphs ? b.active : nullptr;
     const LabelFilter lf{labels, b.gid, active};
     count_triangles(c, o, c.wplan, lf, c.itcount, c.slot_flag, s);
-    k_internal_degrees<<<grid_for(((uint64_t)g.n + g.rows.nchunks) * 32, TPB), TPB, 0, s>>>(
+    k_internal_degrees<<<grid_for(((uint64_t)(g.n + 31) / 32 + g.rows.nchunks) * 32, TPB), TPB, 0, s>>>(
         g.n, g.rows, g.indices, g.nlow, g.adj, c.slot_flag, c.itdeg, lf);
     CK_LAUNCH("k_internal_degrees");
     if (b.blocks) {
