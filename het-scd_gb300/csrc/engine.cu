@@ -61,6 +61,32 @@ __global__ void k_seen_labels(uint32_t n, const uint32_t *__restrict__ labels, u
     }
 }
 
+// compress_labels as intended (src/scd.cpp:32-55 without the inverted branch):
+// in vertex order, an unlabelled vertex or the first vertex of a label opens the
+// next community id; later vertices of a label take its id
+__global__ void k_first_of_label(uint32_t n, const uint32_t *__restrict__ labels, uint32_t *first) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t l = labels[v];
+        if (l != INVALID) atomicMin(first + l, v);
+    }
+}
+
+struct OpensCommunity {
+    const uint32_t *labels, *first;
+    __device__ uint32_t operator[](size_t v) const {
+        const uint32_t l = labels[v];
+        return l == INVALID || first[l] == (uint32_t)v;
+    }
+};
+
+__global__ void k_compressed(uint32_t n, const uint32_t *__restrict__ labels, const uint32_t *__restrict__ first,
+                             const uint32_t *__restrict__ rank, uint32_t *out) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t l = labels[v];
+        out[v] = rank[l == INVALID ? v : first[l]];
+    }
+}
+
 __global__ void k_distinct_per_graph(uint32_t G, const uint32_t *__restrict__ comm_off, const uint32_t *__restrict__ scan,
                                      uint32_t *out) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x)
@@ -730,6 +756,31 @@ int scd_current_labels(scd_ctx *ctx, uint32_t *labels) {
         require_labels(c);
         if (c.g.n) CK(cudaMemcpyAsync(labels, c.labels, (size_t)c.g.n * 4, cudaMemcpyDeviceToHost, c.stream));
         CK(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int scd_compressed_labels(scd_ctx *ctx, uint32_t *labels, uint32_t *num_communities) {
+    return guarded(ctx, [&](Ctx &c) {
+        require_labels(c);
+        if (c.b.G != 1) throw Error(SCD_ERR_STATE, "the context holds a batch: compressed labels are per single graph");
+        cudaStream_t s = c.stream;
+        const uint32_t n = c.g.n;
+        uint32_t total = 0;
+        if (n) {
+            const uint32_t nc = c.num_comms ? c.num_comms : 1;
+            DevBuf<uint32_t> first(nc, s), rank((size_t)n + 1, s), out(n, s);
+            CK(cudaMemsetAsync(first.get(), 0xff, (size_t)nc * 4, s));
+            k_first_of_label<<<grid_for(n, TPB), TPB, 0, s>>>(n, c.best, first.get());
+            CK_LAUNCH("k_first_of_label");
+            scan_exclusive<uint32_t>(OpensCommunity{c.best, first.get()}, rank.get(), n, s);
+            k_compressed<<<grid_for(n, TPB), TPB, 0, s>>>(n, c.best, first.get(), rank.get(), out.get());
+            CK_LAUNCH("k_compressed");
+            c.launches += 3;
+            CK(cudaMemcpyAsync(&total, rank.get() + n, 4, cudaMemcpyDeviceToHost, s));
+            if (labels) CK(cudaMemcpyAsync(labels, out.get(), (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+        }
+        if (num_communities) *num_communities = total;
     });
 }
 

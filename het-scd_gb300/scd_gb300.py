@@ -79,6 +79,7 @@ def lib():
             "scd_batch_labels": ([P, u32, P], i32),
             "scd_batch_convert_lists": ([P, P, P, u32], i32),
             "scd_convert_text": ([P, ctypes.c_char_p, u64, i32], i32),
+            "scd_compressed_labels": ([P, P, ctypes.POINTER(u32)], i32),
             "scd_parse_text": ([P, ctypes.c_char_p, u64, i32, P, ctypes.POINTER(u64)], i32),
             "scd_batch_labels_all": ([P, P, P], i32),
             "scd_autotune": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(dbl),
@@ -208,6 +209,14 @@ class Engine:
         out = np.empty(n, np.uint32)
         self._check(lib().scd_labels_from_device(self._ctx, _p(out)))
         return out
+
+    def compressed_labels(self):
+        """The best labels renumbered as compress_labels intends; returns (labels, count)."""
+        n = self.graph_info()[0]
+        out = np.empty(max(n, 1), np.uint32)
+        k = ctypes.c_uint32()
+        self._check(lib().scd_compressed_labels(self._ctx, _p(out), ctypes.byref(k)))
+        return out[:n], k.value
 
     def current_labels(self):
         n = self.graph_info()[0]

@@ -121,6 +121,12 @@ int scd_labels_from_device(scd_ctx *ctx, uint32_t *labels);
  * NULL; arrays hold *num_communities entries.  Statistics are for a single graph
  * (SCD_ERR_STATE on a batch: converged graphs of a batch stop updating theirs). */
 int scd_current_labels(scd_ctx *ctx, uint32_t *labels);
+/* compress_labels (src/scd.cpp:32-55) as its code intends, without the inverted
+ * branch: the best labels renumbered in vertex order (an unlabelled vertex or the
+ * first vertex of a label opens the next id, later vertices of the label take it);
+ * labels (nullable) receives n entries, *num_communities the number of ids.
+ * Single-graph contexts. */
+int scd_compressed_labels(scd_ctx *ctx, uint32_t *labels, uint32_t *num_communities);
 int scd_community_stats(scd_ctx *ctx, int32_t *sizes, int32_t *ext_edges, int32_t *int_edges,
                         uint32_t *num_communities);
 

@@ -148,6 +148,33 @@ def test_transferred_graph_with_isolated_vertices(engine):
         assert rel(w, ref["wcc"][i]) < WCC_RTOL
 
 
+def _compress_intended(labels):
+    """compress_labels (src/scd.cpp:32-55) with its branch the way round it is meant."""
+    out, seen, k = np.empty_like(labels), {}, 0
+    for p, l in enumerate(labels.tolist()):
+        if l == 0xFFFFFFFF:
+            out[p] = k
+            k += 1
+        elif l not in seen:
+            seen[l] = k
+            out[p] = k
+            k += 1
+        else:
+            out[p] = seen[l]
+    return out, k
+
+
+@pytest.mark.parametrize("name", ["planted_2k_mu03", "chunglu_20k", "rmat_12"])
+def test_compressed_labels(engine, name):
+    engine.transfer_graph(O.Graph.from_bytes(G.graph_bytes(name)))
+    r = engine.run(0.01, 1000)
+    best = engine.labels_from_device()
+    got, k = engine.compressed_labels()
+    want, kw = _compress_intended(best)
+    assert k == kw and np.array_equal(got, want)
+    assert k == r["distinct_communities"] + int((best == 0xFFFFFFFF).sum())
+
+
 def test_call_order_and_argument_errors(engine):
     e = S.Engine(0)
     with pytest.raises(S.ScdError) as ex:
