@@ -359,7 +359,7 @@ void finish_graph(Ctx &c) {
     c.slot_flag = c.alloc<uint8_t>(2 * (size_t)g.m);
     c.itcount = c.alloc<uint32_t>(n);
     c.itdeg = c.alloc<int32_t>(n);
-    if (n) tc_plan(c, Oriented{g.indices, g.nlow, g.adj, n}, c.wplan, s, true);
+    if (n) tc_plan(c, Oriented{g.indices, g.nlow, g.adj, n}, c.wplan, s, true, false);
     c.wcc_part = c.alloc<double>(b.blocks + 1);
     compute_p_ext(c);
     c.launches += 4;
@@ -1017,7 +1017,7 @@ int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t
         const double ms = autotune_tc(c, &lines);
         if (c.g.n) {   // the WCC plan follows the chosen split
             c.wplan = TcPlan();
-            tc_plan(c, Oriented{c.g.indices, c.g.nlow, c.g.adj, c.g.n}, c.wplan, c.stream, true);
+            tc_plan(c, Oriented{c.g.indices, c.g.nlow, c.g.adj, c.g.n}, c.wplan, c.stream, true, false);
         }
         if (small_max) *small_max = c.tc_small;
         if (warp_max) *warp_max = c.tc_b0;

@@ -107,6 +107,15 @@ struct Oriented {
     const uint32_t *len;   // and has len[u] entries (sorted ascending by id)
     const uint32_t *adj;
     uint32_t n;
+    // in-lists (the v with u in out(v)): iadj[ibeg[u], ibeg[u] + ilen[u]); without
+    // ibeg, beg is the offset array of a symmetric CSR whose rows hold the
+    // out-list first and the in-list after it
+    const uint32_t *ibeg = nullptr, *ilen = nullptr, *iadj = nullptr;
+    __device__ __forceinline__ uint32_t in_beg(uint32_t u) const { return ibeg ? ibeg[u] : beg[u] + len[u]; }
+    __device__ __forceinline__ uint32_t in_len(uint32_t u) const {
+        return ibeg ? ilen[u] : beg[u + 1] - beg[u] - len[u];
+    }
+    __device__ __forceinline__ const uint32_t *in_adj() const { return ibeg ? iadj : adj; }
 };
 // Label mode of triangle counting: only triangles whose three vertices carry
 // the same valid label count; with `active`, vertices of graphs of a batch that
@@ -118,15 +127,21 @@ struct LabelFilter {
     __device__ __forceinline__ bool frozen(uint32_t v) const { return active && !active[gid[v]]; }
 };
 // out-degree buckets and their work-unit offsets (built once per oriented graph)
+// Bucket k lists its out-list centres first (nfwd[k] of them) and, for the CTA
+// buckets, then the in-list centres: a vertex b whose edges a -> b with
+// d+(a) < d+(b) (b-centric edges, below) are counted from b's table.
 struct TcPlan {
     static constexpr int K = 6;
     uint32_t *verts[K] = {};
     uint32_t *unit_off[K] = {};
     uint32_t nverts[K] = {};
+    uint32_t nfwd[K] = {};
+    uint32_t dir_lo = 0, dir_hi = 0;   // b-centric iff d+(a) < d+(b) and dir_lo < d+(b) <= dir_hi
     DevBuf<uint32_t> tmp[2 * K];   // storage when the plan is temporary
 };
 struct Ctx;
-void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned);
+// in_lists: also in-list centres (b-centric edges) in the CTA buckets
+void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists);
 // tcount[v] += triangles at v; flag[slot] = 1 for out-slots on a triangle.
 // With labels: internal triangles only.  tcount and flag must be zeroed.
 // Sorts every row of a CSR (offsets off[nrows+1], values vals) ascending in place;

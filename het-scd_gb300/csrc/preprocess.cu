@@ -112,24 +112,30 @@ struct IsOut {
     }
 };
 
+// out-slots (u, v) to orow/ocol at pos[i]; in-slots (v -> u) to icol at i - pos[i]
+// (both keep the row order, so out- and in-lists stay sorted)
 __global__ void k_orient(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
                          const uint32_t *__restrict__ indices, uint32_t count,
-                         const uint32_t *__restrict__ pos, uint32_t *orow, uint32_t *ocol) {
+                         const uint32_t *__restrict__ pos, uint32_t *orow, uint32_t *ocol, uint32_t *icol) {
     IsOut f{rows, cols, indices};
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         if (f[i]) {
             orow[pos[i]] = rows[i];
             ocol[pos[i]] = cols[i];
+        } else {
+            icol[i - pos[i]] = cols[i];
         }
     }
 }
 
 __global__ void k_out_ranges(const uint32_t *__restrict__ indices, const uint32_t *__restrict__ pos,
-                             uint32_t n, uint32_t *obeg, uint32_t *olen) {
+                             uint32_t n, uint32_t *obeg, uint32_t *olen, uint32_t *ibeg, uint32_t *ilen) {
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-        uint32_t b = pos[indices[u]], e = pos[indices[u + 1]];
+        const uint32_t r0 = indices[u], r1 = indices[u + 1], b = pos[r0], e = pos[r1];
         obeg[u] = b;
         olen[u] = e - b;
+        ibeg[u] = r0 - b;
+        ilen[u] = (r1 - r0) - (e - b);
     }
 }
 
@@ -430,10 +436,12 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     DevBuf<uint32_t> opos(slots1 + 1, s);
     scan_exclusive<uint32_t>(IsOut{rows1.get(), cols1.get(), ind1.get()}, opos.get(), slots1, s);
     DevBuf<uint32_t> orow(m1, s), ocol(m1, s), obeg(n1, s), olen(n1, s);
+    DevBuf<uint32_t> icol(m1 ? m1 : 1, s), ibeg(n1, s), ilen(n1, s);
     k_orient<<<grid_for(slots1, TPB), TPB, 0, s>>>(rows1.get(), cols1.get(), ind1.get(), slots1, opos.get(),
-                                                  orow.get(), ocol.get());
+                                                  orow.get(), ocol.get(), icol.get());
     CK_LAUNCH("k_orient");
-    k_out_ranges<<<grid_for(n1, TPB), TPB, 0, s>>>(ind1.get(), opos.get(), n1, obeg.get(), olen.get());
+    k_out_ranges<<<grid_for(n1, TPB), TPB, 0, s>>>(ind1.get(), opos.get(), n1, obeg.get(), olen.get(), ibeg.get(),
+                                                   ilen.get());
     CK_LAUNCH("k_out_ranges");
     opos.release();
     rows1.release();
@@ -443,12 +451,15 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     DevBuf<uint8_t> oflag(m1, s);
     CK(cudaMemsetAsync(tcount.get(), 0, (size_t)n1 * 4, s));
     CK(cudaMemsetAsync(oflag.get(), 0, m1, s));
-    Oriented o{obeg.get(), olen.get(), ocol.get(), n1};
+    Oriented o{obeg.get(), olen.get(), ocol.get(), n1, ibeg.get(), ilen.get(), icol.get()};
     {
         TcPlan plan;
-        tc_plan(c, o, plan, s, false);
+        tc_plan(c, o, plan, s, false, true);
         count_triangles(c, o, plan, LabelFilter{}, tcount.get(), oflag.get(), s);
     }
+    icol.release();
+    ibeg.release();
+    ilen.release();
     DevBuf<int32_t> tri1(n1, s), tdeg1(n1, s);
     CK(cudaMemsetAsync(tdeg1.get(), 0, (size_t)n1 * 4, s));
     k_tri_from_count<<<grid_for(n1, TPB), TPB, 0, s>>>(tcount.get(), n1, tri1.get());

@@ -20,8 +20,15 @@
 // of flagged edges (src/wcc.cpp:84-127).  Only b and the table entries c with
 // a's label take part, so every hit is an internal triangle.
 //
+// Which vertex's table counts a triangle: an edge a -> b whose b has the longer
+// out-list (d+(a) < d+(b), b in the CTA buckets) is b-centric: instead of
+// walking out(b) against a's table, the unit of b walks out(a) against b's
+// table (b's in-lists give the a).  Every triangle a -> b -> c is still found
+// exactly once, at a's table or at b's, and the walk is min(d+(a), d+(b))
+// items instead of d+(b) (on R-MAT graphs less than half).
+//
 // Work unit = (vertex a, up to 32 consecutive b of out(a)) for one warp, or
-// (a, up to 256 b) for one CTA when out(a) is long.  out(a) is staged in a
+// (centre, up to 512 partners) for one CTA when the centre's out-list is long.  out(a) is staged in a
 // shared-memory open-addressing table (load <= 1/4 for short lists); the
 // unit's items (b, c in out(b)) are flattened with a prefix sum; a warp takes
 // 256 consecutive items, lane L every 32nd from L (coalesced loads), walking
@@ -39,16 +46,30 @@ constexpr int ITEMS = 8;   // consecutive items per thread
 
 constexpr uint32_t HASH_MUL = 0x9E3779B1u;   // multiplicative hash: table index = top bits
 
+// a -> b (d+(a), d+(b)) is counted at b's table iff d+(a) < d+(b) and lo < d+(b) <= hi
+struct Dir {
+    uint32_t lo, hi;
+    __device__ __forceinline__ bool bcentric(uint32_t da, uint32_t db) const { return da < db && db > lo && db <= hi; }
+};
+
+// units of the centres verts[i]: out-list centres (i < nfwd) have d+ partners, in-list centres their in-degree
 struct UnitsOf {
-    const uint32_t *verts, *len;
-    uint32_t per_unit;
-    __device__ uint32_t operator[](size_t i) const { return (len[verts[i]] + per_unit - 1) / per_unit; }
+    Oriented o;
+    const uint32_t *verts;
+    uint32_t per_unit, nfwd;
+    __device__ uint32_t operator[](size_t i) const {
+        const uint32_t v = verts[i], p = i < nfwd ? o.len[v] : o.in_len(v);
+        return (p + per_unit - 1) / per_unit;
+    }
 };
 
 struct InBucket {
-    const uint32_t *len;
+    Oriented o;
     uint32_t lo, hi;
-    __device__ uint32_t operator[](size_t v) const { return len[v] > lo && len[v] <= hi; }
+    bool in_list;   // in-list centres: also a non-empty in-list
+    __device__ uint32_t operator[](size_t v) const {
+        return o.len[v] > lo && o.len[v] <= hi && (!in_list || o.in_len((uint32_t)v) > 0);
+    }
 };
 
 __global__ void k_bucket_scatter(uint32_t n, InBucket f, const uint32_t *__restrict__ pos, uint32_t *out) {
@@ -67,8 +88,8 @@ __global__ void k_bucket_scatter(uint32_t n, InBucket f, const uint32_t *__restr
 // out(a) entry in out(b) instead (alen searches of log2 d+(b) steps).
 template <int G>
 __global__ void __launch_bounds__(256)
-k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, LabelFilter lf, uint32_t *tcount,
-           uint8_t *flag) {
+k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, Dir dir, LabelFilter lf,
+           uint32_t *tcount, uint8_t *flag) {
     constexpr int PER_WARP = 32 / G;
     __shared__ uint32_t acc[8][32];
     const uint32_t *labels = lf.labels;
@@ -89,7 +110,9 @@ k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, Labe
         const bool in_a = (uint32_t)gl < alen;
         const uint32_t x = in_a ? o.adj[abeg + gl] : 0xffffffffu;
         const bool ok = in_a && (!labels || labels[x] == la);   // usable as b and as c
-        const uint32_t wfull = ok ? o.len[x] : 0u, bb = ok ? o.beg[x] : 0u;
+        const uint32_t dx = ok ? o.len[x] : 0u;
+        const bool walk = ok && !dir.bcentric(alen, dx);        // a -> x is counted here
+        const uint32_t wfull = walk ? dx : 0u, bb = walk ? o.beg[x] : 0u;
         // a long out(b) is searched for the entries of out(a) (below) instead of walked
         const bool far = wfull >= 32 && wfull >= 4 * alen;
         const uint32_t wb = far ? 0u : wfull;
@@ -178,7 +201,7 @@ k_tc_small(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, Labe
 template <int WARPS, int TCAP, int LCAP, int FBITS>
 __global__ void __launch_bounds__(WARPS * 32)
 k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off, uint32_t nverts,
-          LabelFilter lf, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+          Dir dir, LabelFilter lf, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
     const uint32_t *labels = lf.labels;
     __shared__ uint32_t filt[WARPS][(1 << FBITS) / 32];
     __shared__ uint32_t keys[WARPS][TCAP];
@@ -225,8 +248,9 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
         uint32_t wb = 0, bb = 0, b = 0;
         if (j < alen) {
             b = o.adj[abeg + j];
-            if (!labels || labels[b] == la) {
-                wb = o.len[b];
+            const uint32_t db = o.len[b];
+            if ((!labels || labels[b] == la) && !dir.bcentric(alen, db)) {
+                wb = db;
                 bb = o.beg[b];
             }
         }
@@ -297,11 +321,19 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
     }
 }
 
-// CTA units for longer out-lists: (a, up to THREADS b), one shared table per CTA.
-template <int THREADS, int TCAP, int LCAP, int FBITS>
+// CTA units for longer out-lists: (centre x, up to THREADS x ROUNDS partners),
+// one shared table of out(x) per CTA, partners THREADS at a time.  Out-list
+// centres (vi < nfwd) take the partners b = out(x)[j] of edges x -> b counted at
+// x and walk out(b); in-list centres take the a = in(x)[j] of b-centric edges
+// a -> x and walk out(a).  A hit c closes the triangle (x, partner, c): the
+// walked slot is flagged at once, the partner's and the table entry's counts
+// and flags are aggregated in shared memory.  The out-slot of a -> x (in-list
+// centre) is found by a binary search of x in out(a), for partners with hits.
+template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS>
 __global__ void __launch_bounds__(THREADS)
 k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off, uint32_t nverts,
-         LabelFilter lf, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+         uint32_t nfwd, Dir dir, LabelFilter lf, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
+    constexpr uint32_t PER_UNIT = (uint32_t)THREADS * ROUNDS;
     const uint32_t *labels = lf.labels;
     extern __shared__ uint32_t sm[];
     uint32_t *keys = sm;                                  // TCAP
@@ -324,22 +356,23 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
             else hi = mid;
         }
         const uint32_t vi = lo - 1;
-        const uint32_t a = verts[vi], ch = unit - unit_off[vi];
-        const uint32_t la = labels ? labels[a] : 0u;
-        if (labels && (la == INVALID || lf.frozen(a))) {
+        const uint32_t x = verts[vi], ch = unit - unit_off[vi];
+        const bool fwd = vi < nfwd;
+        const uint32_t la = labels ? labels[x] : 0u;
+        if (labels && (la == INVALID || lf.frozen(x))) {
             __syncthreads();
             continue;
         }
-        const uint32_t abeg = o.beg[a], alen = o.len[a];
+        const uint32_t xbeg = o.beg[x], xlen = o.len[x];
         int bits = 1;
-        while ((1u << bits) < 2 * alen) bits++;
+        while ((1u << bits) < 2 * xlen) bits++;
         const uint32_t tmask = (1u << bits) - 1;
         for (uint32_t i = threadIdx.x; i < (1u << bits); i += THREADS) keys[i] = EMPTY;
         for (uint32_t i = threadIdx.x; i < (1u << FBITS) / 32; i += THREADS) filt[i] = 0;
-        for (uint32_t i = threadIdx.x; i < alen; i += THREADS) cnt[i] = 0;
+        for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) cnt[i] = 0;
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < alen; i += THREADS) {
-            const uint32_t id = o.adj[abeg + i];
+        for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) {
+            const uint32_t id = o.adj[xbeg + i];
             if (labels && labels[id] != la) continue;   // only internal c can close an internal triangle
             const uint32_t hv = id * HASH_MUL, fi = hv >> (32 - FBITS);
             atomicOr(&filt[fi >> 5], 1u << (fi & 31));
@@ -347,91 +380,101 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
             while (atomicCAS(&keys[h], EMPTY, id) != EMPTY) h = (h + 1) & tmask;
             idxs[h] = (uint16_t)i;
         }
-        const uint32_t j = ch * THREADS + threadIdx.x;
-        uint32_t wb = 0, bb = 0, b = 0;
-        if (j < alen) {
-            b = o.adj[abeg + j];
-            if (!labels || labels[b] == la) {
-                wb = o.len[b];
-                bb = o.beg[b];
+        const uint32_t *padj = fwd ? o.adj : o.in_adj();
+        const uint32_t pbeg = fwd ? xbeg : o.in_beg(x), plen = fwd ? xlen : o.in_len(x);
+        const uint32_t pend = min(plen, (ch + 1) * PER_UNIT);
+        uint32_t xhits = 0;
+        for (uint32_t r0 = ch * PER_UNIT; r0 < pend; r0 += THREADS) {
+            const uint32_t j = r0 + threadIdx.x;
+            uint32_t wb = 0, bb = 0, y = 0;
+            if (j < pend) {
+                y = padj[pbeg + j];
+                const uint32_t dy = o.len[y];
+                const bool here = fwd ? !dir.bcentric(xlen, dy) : dir.bcentric(dy, xlen);
+                if (here && (!labels || labels[y] == la)) {
+                    wb = dy;
+                    bb = o.beg[y];
+                }
             }
-        }
-        uint32_t incl = warp_inclusive_scan(wb);   // block inclusive scan of wb
-        if (lane == 31) wsum[w] = incl;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t run = 0;
-            for (int k = 0; k < THREADS / 32; k++) {
-                const uint32_t x = wsum[k];
-                wsum[k] = run;
-                run += x;
+            uint32_t incl = warp_inclusive_scan(wb);   // block inclusive scan of wb
+            if (lane == 31) wsum[w] = incl;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t run = 0;
+                for (int k = 0; k < THREADS / 32; k++) {
+                    const uint32_t v = wsum[k];
+                    wsum[k] = run;
+                    run += v;
+                }
+                s_total = run;
             }
-            s_total = run;
-        }
-        __syncthreads();
-        incl += wsum[w];
-        pre[threadIdx.x] = incl - wb;
-        bbase[threadIdx.x] = bb;
-        bhits[threadIdx.x] = 0;
-        const uint32_t total = s_total;
-        __syncthreads();
-        // warp chunks of 32*ITEMS consecutive items; lane L takes items chunk + L + 32k
-        // (coalesced loads) and walks the owner boundaries forward
-        for (uint32_t t0 = (uint32_t)w * 32 * ITEMS; t0 < total; t0 += THREADS * ITEMS) {
-            const uint32_t tl = t0 + lane;
-            uint32_t l0 = 0, l1 = THREADS;   // owner of tl: last thread with pre <= tl
-            while (l0 < l1) {
-                const uint32_t mid = (l0 + l1) >> 1;
-                if (pre[mid] <= tl) l0 = mid + 1;
-                else l1 = mid;
-            }
-            uint32_t jb = l0 - 1;
-            uint32_t nxt = jb + 1 < THREADS ? pre[jb + 1] : total;
-            uint32_t cbase = bbase[jb] - pre[jb];
-            uint32_t cpos[ITEMS], cv[ITEMS], own[ITEMS];
+            __syncthreads();
+            incl += wsum[w];
+            pre[threadIdx.x] = incl - wb;
+            bbase[threadIdx.x] = bb;
+            bhits[threadIdx.x] = 0;
+            const uint32_t total = s_total;
+            __syncthreads();
+            // warp chunks of 32*ITEMS consecutive items; lane L takes items chunk + L + 32k
+            // (coalesced loads) and walks the owner boundaries forward
+            for (uint32_t t0 = (uint32_t)w * 32 * ITEMS; t0 < total; t0 += THREADS * ITEMS) {
+                const uint32_t tl = t0 + lane;
+                uint32_t l0 = 0, l1 = THREADS;   // owner of tl: last thread with pre <= tl
+                while (l0 < l1) {
+                    const uint32_t mid = (l0 + l1) >> 1;
+                    if (pre[mid] <= tl) l0 = mid + 1;
+                    else l1 = mid;
+                }
+                uint32_t jb = l0 - 1;
+                uint32_t nxt = jb + 1 < THREADS ? pre[jb + 1] : total;
+                uint32_t cbase = bbase[jb] - pre[jb];
+                uint32_t cpos[ITEMS], cv[ITEMS], own[ITEMS];
 #pragma unroll
-            for (int k = 0; k < ITEMS; k++) {
-                const uint32_t t = tl + 32 * k;
-                own[k] = INVALID;
-                if (t < total) {
-                    while (t >= nxt) {
-                        jb++;
-                        nxt = jb + 1 < THREADS ? pre[jb + 1] : total;
-                        cbase = bbase[jb] - pre[jb];
+                for (int k = 0; k < ITEMS; k++) {
+                    const uint32_t t = tl + 32 * k;
+                    own[k] = INVALID;
+                    if (t < total) {
+                        while (t >= nxt) {
+                            jb++;
+                            nxt = jb + 1 < THREADS ? pre[jb + 1] : total;
+                            cbase = bbase[jb] - pre[jb];
+                        }
+                        own[k] = jb;
+                        cpos[k] = cbase + t;
+                        cv[k] = o.adj[cpos[k]];
                     }
-                    own[k] = jb;
-                    cpos[k] = cbase + t;
-                    cv[k] = o.adj[cpos[k]];
                 }
-            }
 #pragma unroll
-            for (int k = 0; k < ITEMS; k++) {
-                if (own[k] == INVALID) continue;
-                const uint32_t c = cv[k];
-                const uint32_t hv = c * HASH_MUL, fi = hv >> (32 - FBITS);
-                if (!((filt[fi >> 5] >> (fi & 31)) & 1u)) continue;   // certainly not in out(a)
-                uint32_t h = hv >> (32 - bits), key;
-                while ((key = keys[h]) != c && key != EMPTY) h = (h + 1) & tmask;
-                if (key == c) {
-                    atomicAdd(&cnt[idxs[h]], 1u);
-                    atomicAdd(&bhits[own[k]], 1u);
-                    flag[cpos[k]] = 1;
+                for (int k = 0; k < ITEMS; k++) {
+                    if (own[k] == INVALID) continue;
+                    const uint32_t c = cv[k];
+                    const uint32_t hv = c * HASH_MUL, fi = hv >> (32 - FBITS);
+                    if (!((filt[fi >> 5] >> (fi & 31)) & 1u)) continue;   // certainly not in out(x)
+                    uint32_t h = hv >> (32 - bits), key;
+                    while ((key = keys[h]) != c && key != EMPTY) h = (h + 1) & tmask;
+                    if (key == c) {
+                        atomicAdd(&cnt[idxs[h]], 1u);
+                        atomicAdd(&bhits[own[k]], 1u);
+                        flag[cpos[k]] = 1;
+                    }
                 }
             }
+            __syncthreads();
+            const uint32_t hb = j < pend ? bhits[threadIdx.x] : 0;
+            if (hb) {
+                atomicAdd(tcount + y, hb);
+                const uint32_t yb = o.beg[y];
+                flag[fwd ? xbeg + j : yb + lower_bound(o.adj + yb, o.len[y], x)] = 1;
+            }
+            xhits += hb;
         }
-        __syncthreads();
-        const uint32_t hb = j < alen ? bhits[threadIdx.x] : 0;
-        if (hb) {
-            atomicAdd(tcount + b, hb);
-            flag[abeg + j] = 1;
-        }
-        const uint32_t sa = warp_sum(hb);
-        if (lane == 0 && sa) atomicAdd(tcount + a, sa);
-        for (uint32_t i = threadIdx.x; i < alen; i += THREADS) {
+        const uint32_t sa = warp_sum(xhits);
+        if (lane == 0 && sa) atomicAdd(tcount + x, sa);
+        for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) {
             const uint32_t cc = cnt[i];
             if (cc) {
-                atomicAdd(tcount + o.adj[abeg + i], cc);
-                flag[abeg + i] = 1;
+                atomicAdd(tcount + o.adj[xbeg + i], cc);
+                flag[xbeg + i] = 1;
             }
         }
         __syncthreads();
@@ -443,21 +486,25 @@ constexpr size_t tc_cta_smem() {
     return (size_t)TCAP * 4 + (size_t)LCAP * 4 + ((size_t)1 << FBITS) / 8 + (size_t)TCAP * 2;
 }
 
-template <int THREADS, int TCAP, int LCAP, int FBITS>
+template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS>
 void set_tc_attr() {
     if (tc_cta_smem<TCAP, LCAP, FBITS>() > 48 * 1024)
-        CK(cudaFuncSetAttribute((const void *)k_tc_cta<THREADS, TCAP, LCAP, FBITS>,
+        CK(cudaFuncSetAttribute((const void *)k_tc_cta<THREADS, ROUNDS, TCAP, LCAP, FBITS>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_cta_smem<TCAP, LCAP, FBITS>()));
 }
 
-template <int THREADS, int TCAP, int LCAP, int FBITS>
+template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS>
 void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, LabelFilter labels, uint32_t *tcount,
                    uint8_t *flag, uint32_t *ctr, unsigned grid, cudaStream_t s) {
     const size_t smem = tc_cta_smem<TCAP, LCAP, FBITS>();
-    k_tc_cta<THREADS, TCAP, LCAP, FBITS><<<grid, THREADS, smem, s>>>(o, plan.verts[k], plan.unit_off[k], plan.nverts[k],
-                                                            labels, tcount, flag, ctr);
+    k_tc_cta<THREADS, ROUNDS, TCAP, LCAP, FBITS><<<grid, THREADS, smem, s>>>(
+        o, plan.verts[k], plan.unit_off[k], plan.nverts[k], plan.nfwd[k], Dir{plan.dir_lo, plan.dir_hi}, labels,
+        tcount, flag, ctr);
     CK_LAUNCH("k_tc_cta");
 }
+
+// partners per CTA unit of the two CTA buckets
+constexpr int CTA1_THREADS = 128, CTA1_ROUNDS = 4, CTA2_THREADS = 256, CTA2_ROUNDS = 2;
 
 // Lists longer than 8192 (none in the benchmark graphs): items looked up
 // by binary search in the sorted out-list in global memory, per-triangle
@@ -506,18 +553,28 @@ constexpr uint32_t B2 = 8192;
 
 }  // namespace
 
-void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned) {
+void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists) {
     const uint32_t sm = c.tc_small, s16 = sm < 16 ? sm : 16, b0 = c.tc_b0 > sm ? c.tc_b0 : sm;
     const uint32_t bounds[TcPlan::K + 1] = {0, s16, sm, b0, c.tc_b1, B2, 0xffffffffu};
-    const uint32_t per_unit[TcPlan::K] = {1, 1, 32, 128, 256, 1};
+    const uint32_t per_unit[TcPlan::K] = {1, 1, 32, CTA1_THREADS * CTA1_ROUNDS, CTA2_THREADS * CTA2_ROUNDS, 1};
+    const bool split = in_lists && !(c.flags & SCD_FLAG_TC_OUT_ONLY);
+    plan.dir_lo = split ? b0 : 0;
+    plan.dir_hi = split ? B2 : 0;
     for (int k = 0; k < TcPlan::K; k++) {
-        DevBuf<uint32_t> pos((size_t)o.n + 1, s);
-        InBucket f{o.len, bounds[k], bounds[k + 1]};
-        scan_exclusive<uint32_t>(f, pos.get(), o.n, s);
-        uint32_t cnt = 0;
-        CK(cudaMemcpyAsync(&cnt, pos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+        const bool cta = k == 3 || k == 4;
+        const InBucket fa{o, bounds[k], bounds[k + 1], false}, fb{o, bounds[k], bounds[k + 1], true};
+        DevBuf<uint32_t> pos((size_t)o.n + 1, s), ipos(split && cta ? (size_t)o.n + 1 : 1, s);
+        scan_exclusive<uint32_t>(fa, pos.get(), o.n, s);
+        uint32_t na = 0, nb = 0;
+        CK(cudaMemcpyAsync(&na, pos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+        if (split && cta) {
+            scan_exclusive<uint32_t>(fb, ipos.get(), o.n, s);
+            CK(cudaMemcpyAsync(&nb, ipos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+        }
         CK(cudaStreamSynchronize(s));
+        const uint32_t cnt = na + nb;
         plan.nverts[k] = cnt;
+        plan.nfwd[k] = na;
         if (owned) {
             plan.verts[k] = c.alloc<uint32_t>(cnt);
             plan.unit_off[k] = c.alloc<uint32_t>((size_t)cnt + 1);
@@ -527,11 +584,15 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
             plan.verts[k] = plan.tmp[2 * k].get();
             plan.unit_off[k] = plan.tmp[2 * k + 1].get();
         }
-        if (cnt) {
-            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, f, pos.get(), plan.verts[k]);
+        if (na) {
+            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, fa, pos.get(), plan.verts[k]);
             CK_LAUNCH("k_bucket_scatter");
         }
-        scan_exclusive<uint32_t>(UnitsOf{plan.verts[k], o.len, per_unit[k]}, plan.unit_off[k], cnt, s);
+        if (nb) {
+            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, fb, ipos.get(), plan.verts[k] + na);
+            CK_LAUNCH("k_bucket_scatter");
+        }
+        scan_exclusive<uint32_t>(UnitsOf{o, plan.verts[k], per_unit[k], na}, plan.unit_off[k], cnt, s);
     }
 }
 
@@ -540,8 +601,8 @@ void prepare_tc_kernels() {
     int dev = 0;
     CK(cudaGetDevice(&dev));
     if (done_device == dev) return;
-    set_tc_attr<128, 2048, 1024, 14>();
-    set_tc_attr<256, 16384, 8192, 17>();
+    set_tc_attr<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14>();
+    set_tc_attr<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17>();
     done_device = dev;
 }
 
@@ -566,7 +627,7 @@ double autotune_tc(Ctx &c, std::vector<std::string> *report) {
                 c.tc_b0 = b0;
                 c.tc_b1 = b1;
                 TcPlan plan;
-                tc_plan(c, o, plan, s, false);
+                tc_plan(c, o, plan, s, false, true);
                 double ms_min = 1e300;
                 for (int rep = 0; rep < 2; rep++) {
                     CK(cudaMemsetAsync(tcount.get(), 0, (size_t)g.n * 4, s));
@@ -606,30 +667,31 @@ void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter 
     prepare_tc_kernels();
     uint32_t *ctr = c.work_counter;
     CK(cudaMemsetAsync(ctr, 0, 16, s));
+    const Dir dir{plan.dir_lo, plan.dir_hi};
     if (plan.nverts[0]) {
         k_tc_small<16><<<grid_for((uint64_t)plan.nverts[0] * 16, 256, 152 * 8), 256, 0, s>>>(
-            o, plan.verts[0], plan.nverts[0], labels, tcount, flag);
+            o, plan.verts[0], plan.nverts[0], dir, labels, tcount, flag);
         CK_LAUNCH("k_tc_small16");
         c.launches++;
     }
     if (plan.nverts[1]) {
         k_tc_small<32><<<grid_for((uint64_t)plan.nverts[1] * 32, 256, 152 * 8), 256, 0, s>>>(
-            o, plan.verts[1], plan.nverts[1], labels, tcount, flag);
+            o, plan.verts[1], plan.nverts[1], dir, labels, tcount, flag);
         CK_LAUNCH("k_tc_small32");
         c.launches++;
     }
     if (plan.nverts[2]) {
         k_tc_warp<16, 256, 64, 10><<<152 * 4, 16 * 32, 0, s>>>(o, plan.verts[2], plan.unit_off[2], plan.nverts[2],
-                                                           labels, tcount, flag, ctr);
+                                                           dir, labels, tcount, flag, ctr);
         CK_LAUNCH("k_tc_warp64");
         c.launches++;
     }
     if (plan.nverts[3]) {
-        launch_tc_cta<128, 2048, 1024, 14>(o, plan, 3, labels, tcount, flag, ctr + 1, 152 * 12, s);
+        launch_tc_cta<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14>(o, plan, 3, labels, tcount, flag, ctr + 1, 152 * 12, s);
         c.launches++;
     }
     if (plan.nverts[4]) {
-        launch_tc_cta<256, 16384, 8192, 17>(o, plan, 4, labels, tcount, flag, ctr + 2, 152, s);
+        launch_tc_cta<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17>(o, plan, 4, labels, tcount, flag, ctr + 2, 152, s);
         c.launches++;
     }
     if (plan.nverts[5]) {

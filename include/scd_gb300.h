@@ -44,6 +44,9 @@ extern "C" {
                                      of replaying a captured CUDA graph; with SCD_FLAG_PROFILE
                                      this times the iteration phases (captured iterations are
                                      not split into phases) */
+#define SCD_FLAG_TC_OUT_ONLY 8u   /* count every triangle from the out-list table of its
+                                     lowest-ordered vertex (no in-list units); same results,
+                                     slower on skewed graphs */
 
 typedef struct scd_ctx scd_ctx;
 

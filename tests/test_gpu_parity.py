@@ -219,3 +219,20 @@ def test_rmat_full_pipeline_against_oracle(engine, scale):
         w = engine.improve_labels()
         assert np.array_equal(engine.current_labels(), r["labels"][i])
         assert rel(w, r["wcc"][i]) < WCC_RTOL
+
+
+@pytest.mark.parametrize("make", [lambda: scdgen.rmat(16, 16, seed=7),
+                                  lambda: scdgen.chunglu(60_000, 2.1, 5.0, 5000.0, 0.2, 10, 200, seed=5)])
+def test_in_list_units_agree_with_out_list_counting(engine, make):
+    # the same triangles counted from the out-list tables only (no in-list centres)
+    pairs = make()
+    engine.convert_edges(pairs)
+    e2 = S.Engine(0, flags=S.FLAG_TC_OUT_ONLY)
+    try:
+        e2.convert_edges(pairs)
+        assert e2.graph_bytes() == engine.graph_bytes()
+        r1, r2 = engine.run(0.01, 20), e2.run(0.01, 20)
+        assert r1["wcc"] == r2["wcc"] and r1["iterations"] == r2["iterations"]
+        assert np.array_equal(engine.labels_from_device(), e2.labels_from_device())
+    finally:
+        e2.close()
