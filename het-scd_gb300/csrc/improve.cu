@@ -558,24 +558,38 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
         s_own = 0;
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < deg; i += THREADS) {
-        const uint32_t l = a.labels[a.adj[beg + i]];
-        if (l == INVALID) continue;
-        uint32_t h = hash32(l) & mask;
-        while (true) {
-            uint32_t k = keys[h];
-            if (k == INVALID) {
-                k = atomicCAS(keys + h, INVALID, l);
-                if (k == INVALID) {
-                    list[atomicAdd(&s_n, 1u)] = h;   // first occurrence of l
-                    k = l;
+    // LB neighbour labels per thread are gathered before any is inserted, so their
+    // loads overlap instead of one load chain per neighbour
+    constexpr int LB = 4;
+    for (uint32_t i0 = threadIdx.x; i0 < deg; i0 += THREADS * LB) {
+        uint32_t lb[LB];
+#pragma unroll
+        for (int k = 0; k < LB; k++) {
+            const uint32_t i = i0 + k * THREADS;
+            lb[k] = i < deg ? a.adj[beg + i] : INVALID;
+        }
+#pragma unroll
+        for (int k = 0; k < LB; k++) lb[k] = lb[k] != INVALID ? a.labels[lb[k]] : INVALID;
+#pragma unroll
+        for (int k = 0; k < LB; k++) {
+            const uint32_t l = lb[k];
+            if (l == INVALID) continue;
+            uint32_t h = hash32(l) & mask;
+            while (true) {
+                uint32_t key = keys[h];
+                if (key == INVALID) {
+                    key = atomicCAS(keys + h, INVALID, l);
+                    if (key == INVALID) {
+                        list[atomicAdd(&s_n, 1u)] = h;   // first occurrence of l
+                        key = l;
+                    }
                 }
+                if (key == l) {
+                    atomicAdd(vals + h, 1u);
+                    break;
+                }
+                h = (h + 1) & mask;
             }
-            if (k == l) {
-                atomicAdd(vals + h, 1u);
-                break;
-            }
-            h = (h + 1) & mask;
         }
     }
     __syncthreads();
@@ -685,7 +699,7 @@ k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a)
 constexpr int GLOBAL_THREADS = 512;
 
 // tables: per vertex 3*cap words (keys, counts, occupied-entry list)
-__global__ void __launch_bounds__(GLOBAL_THREADS)
+__global__ void __launch_bounds__(GLOBAL_THREADS, 2)
 k_improve_global(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a, uint32_t *tables,
                  const uint64_t *__restrict__ table_off) {
     const Iv al = iv_of(a.alpha);
@@ -722,6 +736,7 @@ void prepare_improve_kernels() {
     int dev = 0;
     CK(cudaGetDevice(&dev));
     if (done_device == dev) return;
+    set_cta_attr<128, 2048>();
     set_cta_attr<256, 4096>();
     set_cta_attr<512, 16384>();
     done_device = dev;
@@ -773,15 +788,19 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
         c.launches++;
     }
     if (k.count[4]) {
-        launch_cta<256, 4096>(k.list[4], k.count[4], a, s, 152 * 7);
+        launch_cta<128, 2048>(k.list[4], k.count[4], a, s, 152 * 16);
         c.launches++;
     }
     if (k.count[5]) {
-        launch_cta<512, 16384>(k.list[5], k.count[5], a, s, 152);
+        launch_cta<256, 4096>(k.list[5], k.count[5], a, s, 152 * 7);
         c.launches++;
     }
     if (k.count[6]) {
-        k_improve_global<<<grid_for(k.count[6], 1, 152 * 2), GLOBAL_THREADS, 0, s>>>(k.list[6], k.count[6], a,
+        launch_cta<512, 16384>(k.list[6], k.count[6], a, s, 152);
+        c.launches++;
+    }
+    if (k.count[7]) {
+        k_improve_global<<<grid_for(k.count[7], 1, 152 * 2), GLOBAL_THREADS, 0, s>>>(k.list[7], k.count[7], a,
                                                                                     c.big_tables, g.big_table_off);
         CK_LAUNCH("k_improve_global");
         c.launches++;
