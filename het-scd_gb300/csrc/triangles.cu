@@ -329,16 +329,21 @@ k_tc_warp(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__rest
 // walked slot is flagged at once, the partner's and the table entry's counts
 // and flags are aggregated in shared memory.  The out-slot of a -> x (in-list
 // centre) is found by a binary search of x in out(a), for partners with hits.
-template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS>
-__global__ void __launch_bounds__(THREADS)
+//
+// The table entries' hit counts are 16-bit halves of shared words (a count is at
+// most the unit's THREADS x ROUNDS partners), which with the register bound lets
+// MIN_CTAS CTAs share an SM.
+template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS, int MIN_CTAS>
+__global__ void __launch_bounds__(THREADS, MIN_CTAS)
 k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off, uint32_t nverts,
          uint32_t nfwd, Dir dir, LabelFilter lf, uint32_t *tcount, uint8_t *flag, uint32_t *next_unit) {
     constexpr uint32_t PER_UNIT = (uint32_t)THREADS * ROUNDS;
+    static_assert(PER_UNIT < 65536, "16-bit hit counts");
     const uint32_t *labels = lf.labels;
     extern __shared__ uint32_t sm[];
     uint32_t *keys = sm;                                  // TCAP
-    uint32_t *cnt = sm + TCAP;                            // LCAP
-    uint32_t *filt = sm + TCAP + LCAP;                    // 2^FBITS bits
+    uint32_t *cnt = sm + TCAP;                            // LCAP 16-bit counts
+    uint32_t *filt = sm + TCAP + LCAP / 2;                // 2^FBITS bits
     uint16_t *idxs = (uint16_t *)(filt + (1 << FBITS) / 32);   // TCAP
     __shared__ uint32_t pre[THREADS], bbase[THREADS], bhits[THREADS], wsum[THREADS / 32];
     __shared__ uint32_t s_unit, s_total;
@@ -369,7 +374,7 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
         const uint32_t tmask = (1u << bits) - 1;
         for (uint32_t i = threadIdx.x; i < (1u << bits); i += THREADS) keys[i] = EMPTY;
         for (uint32_t i = threadIdx.x; i < (1u << FBITS) / 32; i += THREADS) filt[i] = 0;
-        for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) cnt[i] = 0;
+        for (uint32_t i = threadIdx.x; i < (xlen + 1) / 2; i += THREADS) cnt[i] = 0;
         __syncthreads();
         for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) {
             const uint32_t id = o.adj[xbeg + i];
@@ -453,7 +458,8 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
                     uint32_t h = hv >> (32 - bits), key;
                     while ((key = keys[h]) != c && key != EMPTY) h = (h + 1) & tmask;
                     if (key == c) {
-                        atomicAdd(&cnt[idxs[h]], 1u);
+                        const uint32_t ic = idxs[h];
+                        atomicAdd(&cnt[ic >> 1], 1u << ((ic & 1) << 4));
                         atomicAdd(&bhits[own[k]], 1u);
                         flag[cpos[k]] = 1;
                     }
@@ -471,7 +477,7 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
         const uint32_t sa = warp_sum(xhits);
         if (lane == 0 && sa) atomicAdd(tcount + x, sa);
         for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) {
-            const uint32_t cc = cnt[i];
+            const uint32_t cc = (cnt[i >> 1] >> ((i & 1) << 4)) & 0xffffu;
             if (cc) {
                 atomicAdd(tcount + o.adj[xbeg + i], cc);
                 flag[xbeg + i] = 1;
@@ -483,21 +489,21 @@ k_tc_cta(Oriented o, const uint32_t *__restrict__ verts, const uint32_t *__restr
 
 template <int TCAP, int LCAP, int FBITS>
 constexpr size_t tc_cta_smem() {
-    return (size_t)TCAP * 4 + (size_t)LCAP * 4 + ((size_t)1 << FBITS) / 8 + (size_t)TCAP * 2;
+    return (size_t)TCAP * 4 + (size_t)LCAP * 2 + ((size_t)1 << FBITS) / 8 + (size_t)TCAP * 2;
 }
 
-template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS>
+template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS, int MIN_CTAS>
 void set_tc_attr() {
     if (tc_cta_smem<TCAP, LCAP, FBITS>() > 48 * 1024)
-        CK(cudaFuncSetAttribute((const void *)k_tc_cta<THREADS, ROUNDS, TCAP, LCAP, FBITS>,
+        CK(cudaFuncSetAttribute((const void *)k_tc_cta<THREADS, ROUNDS, TCAP, LCAP, FBITS, MIN_CTAS>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc_cta_smem<TCAP, LCAP, FBITS>()));
 }
 
-template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS>
+template <int THREADS, int ROUNDS, int TCAP, int LCAP, int FBITS, int MIN_CTAS>
 void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, LabelFilter labels, uint32_t *tcount,
                    uint8_t *flag, uint32_t *ctr, unsigned grid, cudaStream_t s) {
     const size_t smem = tc_cta_smem<TCAP, LCAP, FBITS>();
-    k_tc_cta<THREADS, ROUNDS, TCAP, LCAP, FBITS><<<grid, THREADS, smem, s>>>(
+    k_tc_cta<THREADS, ROUNDS, TCAP, LCAP, FBITS, MIN_CTAS><<<grid, THREADS, smem, s>>>(
         o, plan.verts[k], plan.unit_off[k], plan.nverts[k], plan.nfwd[k], Dir{plan.dir_lo, plan.dir_hi}, labels,
         tcount, flag, ctr);
     CK_LAUNCH("k_tc_cta");
@@ -601,8 +607,8 @@ void prepare_tc_kernels() {
     int dev = 0;
     CK(cudaGetDevice(&dev));
     if (done_device == dev) return;
-    set_tc_attr<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14>();
-    set_tc_attr<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17>();
+    set_tc_attr<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14, 12>();
+    set_tc_attr<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17, 1>();
     done_device = dev;
 }
 
@@ -687,11 +693,12 @@ void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter 
         c.launches++;
     }
     if (plan.nverts[3]) {
-        launch_tc_cta<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14>(o, plan, 3, labels, tcount, flag, ctr + 1, 152 * 12, s);
+        launch_tc_cta<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14, 12>(o, plan, 3, labels, tcount, flag, ctr + 1, 152 * 12,
+                                                                     s);
         c.launches++;
     }
     if (plan.nverts[4]) {
-        launch_tc_cta<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17>(o, plan, 4, labels, tcount, flag, ctr + 2, 152, s);
+        launch_tc_cta<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17, 1>(o, plan, 4, labels, tcount, flag, ctr + 2, 152, s);
         c.launches++;
     }
     if (plan.nverts[5]) {
