@@ -4,9 +4,11 @@
 // Instead of one global sort of 64-bit (row, value) keys, whose every radix
 // pass moves every entry, the entries are placed by a counting sort on the row
 // (row lengths, offsets, one scatter) and then every row is sorted on its own:
-//   rows of length <= 128     a warp, bitonic network in registers (1, 2 or 4
-//                             values per lane);
-//   129 .. 512, 513 .. 4096   a CTA, bitonic network in shared memory;
+//   rows of length <= 512     a warp, bitonic network in registers and
+//                             shuffles (1, 2, 4, 8 or 16 values per lane);
+//   513 .. 4096               a CTA, 8 values per thread: the stages whose
+//                             partner is in the same warp in registers and
+//                             shuffles, the cross-warp ones in shared memory;
 //   longer rows               one radix sort of (row rank, value) keys.
 // With de-duplication a repeated value of a row becomes INVALID and the number
 // of distinct values of the row is written out; the caller compacts.
@@ -110,34 +112,85 @@ k_sort_rows_warp_e(const uint32_t *__restrict__ list, uint32_t count, const uint
     }
 }
 
-// rows of one list, one CTA per row, bitonic network over the next power of two >= len
-template <int THREADS, uint32_t CAP>
-__global__ void __launch_bounds__(THREADS)
+// rows of one list, one CTA of W warps per row, E values per thread in index
+// order (value index = threadIdx.x * E + i); bitonic network over the next power
+// of two P >= len: stages with partner distance j < E in registers, E <= j < 32E
+// by shuffles, j >= 32E through shared memory (pairs enumerated directly)
+template <int W, int E>
+__global__ void __launch_bounds__(W * 32)
 k_sort_rows_cta(const uint32_t *__restrict__ list, uint32_t count, const uint32_t *__restrict__ off, uint32_t *vals,
                 bool dedup, uint32_t *udeg) {
-    __shared__ uint32_t sh[CAP];
-    __shared__ uint32_t wsum[THREADS / 32];
+    constexpr int THREADS = W * 32;
+    constexpr uint32_t N = (uint32_t)THREADS * E, WSPAN = 32u * E;
+    __shared__ uint32_t sh[N];
+    __shared__ uint32_t wsum[W];
+    const uint32_t base = threadIdx.x * E;
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
         const uint32_t r = list[i], beg = off[r], len = off[r + 1] - beg;
-        uint32_t P = 64;
+        uint32_t P = WSPAN;
         while (P < len) P <<= 1;
         for (uint32_t t = threadIdx.x; t < P; t += THREADS) sh[t] = t < len ? vals[beg + t] : INVALID;
         __syncthreads();
+        uint32_t v[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) v[e] = base + e < P ? sh[base + e] : INVALID;
+        const bool live = base < P;   // warp-uniform: P is a multiple of the warp span
         for (uint32_t k = 2; k <= P; k <<= 1) {
-            for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-                for (uint32_t t = threadIdx.x; t < P; t += THREADS) {
-                    const uint32_t x = t ^ j;
-                    if (x > t) {
+            if (k > WSPAN) {   // distances j >= 32E: shared memory
+                __syncthreads();
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (live) sh[base + e] = v[e];
+                __syncthreads();
+                for (uint32_t j = k >> 1; j >= WSPAN; j >>= 1) {
+                    for (uint32_t q = threadIdx.x; q < P / 2; q += THREADS) {
+                        const uint32_t t = ((q & ~(j - 1)) << 1) | (q & (j - 1)), x = t | j;
                         const uint32_t a = sh[t], b = sh[x];
                         if ((a > b) == ((t & k) == 0)) {
                             sh[t] = b;
                             sh[x] = a;
                         }
                     }
+                    __syncthreads();
                 }
-                __syncthreads();
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (live) v[e] = sh[base + e];
+            }
+            if (!live) continue;
+#pragma unroll
+            for (int j = 16 * E; j >= E; j >>= 1) {   // partner in lane ^ (j / E)
+                if ((uint32_t)j >= k) continue;
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const uint32_t idx = base + e;
+                    const uint32_t o = __shfl_xor_sync(FULL, v[e], j / E);
+                    const bool asc = (idx & k) == 0, low = (idx & j) == 0;
+                    v[e] = (low == asc) ? min(v[e], o) : max(v[e], o);
+                }
+            }
+#pragma unroll
+            for (int j = E / 2; j > 0; j >>= 1) {    // partner in this thread: e ^ j
+                if ((uint32_t)j >= k) continue;
+#pragma unroll
+                for (int e = 0; e < E; e++) {
+                    const int q = e ^ j;
+                    if (q > e) {
+                        const bool asc = ((base + e) & k) == 0;
+                        const uint32_t x = v[e], y = v[q];
+                        if ((x > y) == asc) {
+                            v[e] = y;
+                            v[q] = x;
+                        }
+                    }
+                }
             }
         }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < E; e++)
+            if (live) sh[base + e] = v[e];
+        __syncthreads();
         uint32_t kept = 0;
         for (uint32_t t = threadIdx.x; t < len; t += THREADS) {
             const uint32_t v = sh[t];
@@ -215,8 +268,8 @@ void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool
     CK_LAUNCH("k_sort_rows_warp");
     c.launches++;
     // the longer rows, listed by length class (one host read for all the counts)
-    constexpr int NC = 5;
-    const uint32_t bounds[NC + 1] = {WARP_ROW, 64, 128, MID_ROW, BIG_ROW, 0xffffffffu};
+    constexpr int NC = 7;
+    const uint32_t bounds[NC + 1] = {WARP_ROW, 64, 128, 256, MID_ROW, BIG_ROW, 0xffffffffu};
     DevBuf<uint32_t> pos[NC];
     for (int k = 0; k < NC; k++) {
         pos[k].alloc((size_t)nrows + 1, s);
@@ -247,33 +300,39 @@ void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool
         c.launches++;
     }
     if (cnt[2]) {
-        k_sort_rows_cta<128, MID_ROW><<<grid_for(cnt[2], 1, 152 * 16), 128, 0, s>>>(list[2].get(), cnt[2], off, vals,
-                                                                                 dedup, udeg);
-        CK_LAUNCH("k_sort_rows_cta512");
+        k_sort_rows_warp_e<8><<<grid_for((uint64_t)cnt[2] * 32, TPB), TPB, 0, s>>>(list[2].get(), cnt[2], off, vals,
+                                                                                dedup, udeg);
+        CK_LAUNCH("k_sort_rows_warp256");
         c.launches++;
     }
     if (cnt[3]) {
-        k_sort_rows_cta<512, BIG_ROW><<<grid_for(cnt[3], 1, 152 * 4), 512, 0, s>>>(list[3].get(), cnt[3], off, vals,
-                                                                                dedup, udeg);
-        CK_LAUNCH("k_sort_rows_cta4096");
+        k_sort_rows_warp_e<16><<<grid_for((uint64_t)cnt[3] * 32, TPB), TPB, 0, s>>>(list[3].get(), cnt[3], off, vals,
+                                                                                 dedup, udeg);
+        CK_LAUNCH("k_sort_rows_warp512");
         c.launches++;
     }
     if (cnt[4]) {
-        DevBuf<uint32_t> koff((size_t)cnt[4] + 1, s);
-        scan_exclusive<uint32_t>(RowLenOf{list[4].get(), off}, koff.get(), cnt[4], s);
+        k_sort_rows_cta<BIG_ROW / 256, 8><<<grid_for(cnt[4], 1, 152 * 4), BIG_ROW / 8, 0, s>>>(list[4].get(), cnt[4],
+                                                                                            off, vals, dedup, udeg);
+        CK_LAUNCH("k_sort_rows_cta4096");
+        c.launches++;
+    }
+    if (cnt[5]) {
+        DevBuf<uint32_t> koff((size_t)cnt[5] + 1, s);
+        scan_exclusive<uint32_t>(RowLenOf{list[5].get(), off}, koff.get(), cnt[5], s);
         uint32_t total = 0;
-        CK(cudaMemcpyAsync(&total, koff.get() + cnt[4], 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&total, koff.get() + cnt[5], 4, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         DevBuf<uint64_t> keys(total, s);
-        k_big_keys<<<grid_for(cnt[4], 1, 152 * 8), TPB, 0, s>>>(list[4].get(), cnt[4], off, koff.get(), vals,
+        k_big_keys<<<grid_for(cnt[5], 1, 152 * 8), TPB, 0, s>>>(list[5].get(), cnt[5], off, koff.get(), vals,
                                                                keys.get());
         CK_LAUNCH("k_big_keys");
-        radix_sort<uint64_t>(keys.get(), nullptr, total, 0, 32 + ceil_log2(cnt[4] < 2 ? 2 : cnt[4]), s);
+        radix_sort<uint64_t>(keys.get(), nullptr, total, 0, 32 + ceil_log2(cnt[5] < 2 ? 2 : cnt[5]), s);
         if (udeg) {
-            k_zero_rows<<<grid_for(cnt[4], TPB), TPB, 0, s>>>(list[4].get(), cnt[4], udeg);
+            k_zero_rows<<<grid_for(cnt[5], TPB), TPB, 0, s>>>(list[5].get(), cnt[5], udeg);
             CK_LAUNCH("k_zero_rows");
         }
-        k_big_back<<<grid_for(total, TPB), TPB, 0, s>>>(keys.get(), total, list[4].get(), off, koff.get(), vals,
+        k_big_back<<<grid_for(total, TPB), TPB, 0, s>>>(keys.get(), total, list[5].get(), off, koff.get(), vals,
                                                         dedup, udeg);
         CK_LAUNCH("k_big_back");
         c.launches += 3;
