@@ -6,9 +6,9 @@
 // (row lengths, offsets, one scatter) and then every row is sorted on its own:
 //   rows of length <= 512     a warp, bitonic network in registers and
 //                             shuffles (1, 2, 4, 8 or 16 values per lane);
-//   513 .. 4096               a CTA, 8 values per thread: the stages whose
-//                             partner is in the same warp in registers and
-//                             shuffles, the cross-warp ones in shared memory;
+//   513 .. 4096, .. 16384     a CTA, 8 or 16 values per thread: the stages
+//                             whose partner is in the same warp in registers
+//                             and shuffles, the cross-warp ones in shared memory;
 //   longer rows               one radix sort of (row rank, value) keys.
 // With de-duplication a repeated value of a row becomes INVALID and the number
 // of distinct values of the row is written out; the caller compacts.
@@ -19,7 +19,7 @@ namespace scd {
 namespace {
 
 constexpr unsigned TPB = 256;
-constexpr uint32_t WARP_ROW = 32, MID_ROW = 512, BIG_ROW = 4096;
+constexpr uint32_t WARP_ROW = 32, MID_ROW = 512, BIG_ROW = 4096, HUGE_ROW = 16384;
 
 __device__ __forceinline__ uint32_t bitonic32(uint32_t v, int lane) {
 #pragma unroll
@@ -122,7 +122,7 @@ k_sort_rows_cta(const uint32_t *__restrict__ list, uint32_t count, const uint32_
                 bool dedup, uint32_t *udeg) {
     constexpr int THREADS = W * 32;
     constexpr uint32_t N = (uint32_t)THREADS * E, WSPAN = 32u * E;
-    __shared__ uint32_t sh[N];
+    extern __shared__ uint32_t sh[];   // N values
     __shared__ uint32_t wsum[W];
     const uint32_t base = threadIdx.x * E;
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
@@ -259,6 +259,16 @@ __global__ void k_zero_rows(const uint32_t *__restrict__ list, uint32_t count, u
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) udeg[list[i]] = 0;
 }
 
+void prepare_sort_kernels() {
+    static thread_local int done_device = -1;
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    if (done_device == dev) return;
+    CK(cudaFuncSetAttribute((const void *)k_sort_rows_cta<32, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)(HUGE_ROW * 4)));
+    done_device = dev;
+}
+
 }  // namespace
 
 void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool dedup, uint32_t *udeg,
@@ -268,8 +278,9 @@ void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool
     CK_LAUNCH("k_sort_rows_warp");
     c.launches++;
     // the longer rows, listed by length class (one host read for all the counts)
-    constexpr int NC = 7;
-    const uint32_t bounds[NC + 1] = {WARP_ROW, 64, 128, 256, MID_ROW, BIG_ROW, 0xffffffffu};
+    constexpr int NC = 8;
+    const uint32_t bounds[NC + 1] = {WARP_ROW, 64, 128, 256, MID_ROW, BIG_ROW, HUGE_ROW, 0xffffffffu};
+    prepare_sort_kernels();
     DevBuf<uint32_t> pos[NC];
     for (int k = 0; k < NC; k++) {
         pos[k].alloc((size_t)nrows + 1, s);
@@ -312,27 +323,33 @@ void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool
         c.launches++;
     }
     if (cnt[4]) {
-        k_sort_rows_cta<BIG_ROW / 256, 8><<<grid_for(cnt[4], 1, 152 * 4), BIG_ROW / 8, 0, s>>>(list[4].get(), cnt[4],
-                                                                                            off, vals, dedup, udeg);
+        k_sort_rows_cta<16, 8><<<grid_for(cnt[4], 1, 152 * 4), 512, BIG_ROW * 4, s>>>(list[4].get(), cnt[4], off, vals,
+                                                                                    dedup, udeg);
         CK_LAUNCH("k_sort_rows_cta4096");
         c.launches++;
     }
     if (cnt[5]) {
-        DevBuf<uint32_t> koff((size_t)cnt[5] + 1, s);
-        scan_exclusive<uint32_t>(RowLenOf{list[5].get(), off}, koff.get(), cnt[5], s);
+        k_sort_rows_cta<32, 16><<<grid_for(cnt[5], 1, 152 * 2), 1024, HUGE_ROW * 4, s>>>(list[5].get(), cnt[5], off,
+                                                                                      vals, dedup, udeg);
+        CK_LAUNCH("k_sort_rows_cta16384");
+        c.launches++;
+    }
+    if (cnt[6]) {
+        DevBuf<uint32_t> koff((size_t)cnt[6] + 1, s);
+        scan_exclusive<uint32_t>(RowLenOf{list[6].get(), off}, koff.get(), cnt[6], s);
         uint32_t total = 0;
-        CK(cudaMemcpyAsync(&total, koff.get() + cnt[5], 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&total, koff.get() + cnt[6], 4, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         DevBuf<uint64_t> keys(total, s);
-        k_big_keys<<<grid_for(cnt[5], 1, 152 * 8), TPB, 0, s>>>(list[5].get(), cnt[5], off, koff.get(), vals,
+        k_big_keys<<<grid_for(cnt[6], 1, 152 * 8), TPB, 0, s>>>(list[6].get(), cnt[6], off, koff.get(), vals,
                                                                keys.get());
         CK_LAUNCH("k_big_keys");
-        radix_sort<uint64_t>(keys.get(), nullptr, total, 0, 32 + ceil_log2(cnt[5] < 2 ? 2 : cnt[5]), s);
+        radix_sort<uint64_t>(keys.get(), nullptr, total, 0, 32 + ceil_log2(cnt[6] < 2 ? 2 : cnt[6]), s);
         if (udeg) {
-            k_zero_rows<<<grid_for(cnt[5], TPB), TPB, 0, s>>>(list[5].get(), cnt[5], udeg);
+            k_zero_rows<<<grid_for(cnt[6], TPB), TPB, 0, s>>>(list[6].get(), cnt[6], udeg);
             CK_LAUNCH("k_zero_rows");
         }
-        k_big_back<<<grid_for(total, TPB), TPB, 0, s>>>(keys.get(), total, list[5].get(), off, koff.get(), vals,
+        k_big_back<<<grid_for(total, TPB), TPB, 0, s>>>(keys.get(), total, list[6].get(), off, koff.get(), vals,
                                                         dedup, udeg);
         CK_LAUNCH("k_big_back");
         c.launches += 3;
