@@ -24,7 +24,7 @@ namespace scd {
 // vertex lists by degree: (0,8], (8,16], (16,32], (32,256], (256,2048], (2048,8192], > 8192
 struct DegreeClasses {
     static constexpr int K = 8;
-    static constexpr uint32_t upper[K] = {8, 16, 32, 256, 1024, 2048, 8192, 0xffffffffu};
+    static constexpr uint32_t upper[K] = {8, 16, 32, 256, 1024, 2048, 4096, 0xffffffffu};
     uint32_t *list[K] = {};   // class 0 also holds the isolated vertices (degree 0)
     uint32_t count[K] = {};
 };

@@ -8,8 +8,9 @@
 //                    equal-label set owns the label;
 //   33 .. 256        one warp per vertex, open-addressing (label, count) table
 //                    in shared memory;
-//   257 .. 8192      one CTA per vertex, the table in shared memory (two sizes);
-//   > 8192           one CTA per vertex, per-vertex table in global memory.
+//   257 .. 4096      one CTA per vertex, the table in shared memory (three
+//                    sizes, so that short tables leave room for more CTAs);
+//   > 4096           one CTA per vertex, per-vertex table in global memory.
 // Every distinct label first gets an FP32 interval enclosure of its FP64 gain
 // (gain_interval.cuh); for short label lists the intervals of many vertices are
 // evaluated together, 32 per warp pass.  The intervals settle most vertices:
@@ -738,7 +739,7 @@ void prepare_improve_kernels() {
     if (done_device == dev) return;
     set_cta_attr<128, 2048>();
     set_cta_attr<256, 4096>();
-    set_cta_attr<512, 16384>();
+    set_cta_attr<512, 8192>();
     done_device = dev;
 }
 
@@ -796,7 +797,7 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
         c.launches++;
     }
     if (k.count[6]) {
-        launch_cta<512, 16384>(k.list[6], k.count[6], a, s, 152);
+        launch_cta<512, 8192>(k.list[6], k.count[6], a, s, 152 * 2);
         c.launches++;
     }
     if (k.count[7]) {
