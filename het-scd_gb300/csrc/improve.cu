@@ -536,7 +536,7 @@ k_improve_warp(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a
 // passes touch only the distinct labels.
 template <int THREADS>
 __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, uint32_t *vals, uint32_t *list,
-                            uint32_t cap, double p_ext, Iv pe, Iv al) {
+                            float *hi_of, uint32_t cap, double p_ext, Iv pe, Iv al) {
     __shared__ double s_gain[THREADS / 32];
     __shared__ uint32_t s_label[THREADS / 32];
     __shared__ float s_lo[THREADS / 32], s_hi[THREADS / 32];
@@ -595,7 +595,8 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     }
     __syncthreads();
     const uint32_t nl = s_n;
-    // pass 1: best lower and upper bounds among foreign labels, the own label's interval
+    // pass 1: best lower and upper bounds among foreign labels, the own label's
+    // interval; hi_of[i] keeps label i's upper bound for pass 2 (+inf: unusable)
     float m = -INFINITY, mh = -INFINITY;
     for (uint32_t i = threadIdx.x; i < nl; i += THREADS) {
         const uint32_t h = list[i], l = keys[h];
@@ -604,12 +605,16 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
         if (l == mine) {
             s_own = own_sign_known(iv, need) ? 1 : 2;
             s_own_hi = iv.hi;
+            hi_of[i] = -INFINITY;
             continue;
         }
-        if (need) s_need = 1;
-        else {
+        if (need) {
+            s_need = 1;
+            hi_of[i] = INFINITY;
+        } else {
             m = fmaxf(m, iv.lo);
             mh = fmaxf(mh, iv.hi);
+            hi_of[i] = iv.hi;
         }
     }
 #pragma unroll
@@ -642,9 +647,8 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
             else if (s_own_hi < 0.f) s_remove = 1.0;   // only its sign matters when nothing survives
             continue;
         }
-        bool need = false;
-        const Iv iv = interval_gain(a, l, vals[h], deg, pe, al, &need);
-        if (need || (iv.hi > 0.f && iv.hi >= m)) {
+        const float hi = hi_of[i];
+        if (hi > 0.f && hi >= m) {
             const double g = exact_gain(a, l, vals[h], deg, mine, p_ext);
             if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
                 bg = g;
@@ -682,6 +686,7 @@ __global__ void __launch_bounds__(THREADS)
 k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a) {
     extern __shared__ uint32_t smem[];
     uint32_t *keys = smem, *vals = smem + CAP, *list = smem + 2 * CAP;
+    float *hi_of = (float *)(list + CAP / 2);
     const Iv al = iv_of(a.alpha);
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {
         const uint32_t p = verts[i];
@@ -693,13 +698,14 @@ k_improve_cta(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a)
         const uint32_t deg = a.indices[p + 1] - a.indices[p];
         uint32_t cap = 64;
         while (cap < 2 * deg) cap <<= 1;
-        improve_cta<THREADS>(a, p, keys, vals, list, cap, a.p_ext[gp], pe_of(a, gp), al);
+        improve_cta<THREADS>(a, p, keys, vals, list, hi_of, cap, a.p_ext[gp], pe_of(a, gp), al);
     }
 }
 
 constexpr int GLOBAL_THREADS = 512;
 
-// tables: per vertex 3*cap words (keys, counts, occupied-entry list)
+// tables: per vertex 3*cap words (keys, counts; then the occupied-entry list and
+// the labels' upper bounds, cap / 2 each)
 __global__ void __launch_bounds__(GLOBAL_THREADS, 2)
 k_improve_global(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs a, uint32_t *tables,
                  const uint64_t *__restrict__ table_off) {
@@ -714,20 +720,20 @@ k_improve_global(const uint32_t *__restrict__ verts, uint32_t count, ImproveArgs
         const uint64_t off = table_off[i];
         const uint32_t cap = (uint32_t)((table_off[i + 1] - off) / 3);
         uint32_t *t = tables + off;
-        improve_cta<GLOBAL_THREADS>(a, p, t, t + cap, t + 2 * cap, cap, a.p_ext[gp], pe_of(a, gp), al);
+        improve_cta<GLOBAL_THREADS>(a, p, t, t + cap, t + 2 * cap, (float *)(t + 2 * cap + cap / 2), cap, a.p_ext[gp],
+                                    pe_of(a, gp), al);
     }
 }
 
 template <int THREADS, uint32_t CAP>
-constexpr size_t cta_smem() {
-    return (2 * CAP + CAP / 2) * sizeof(uint32_t);
+constexpr size_t cta_smem() {   // keys, counts (CAP each), entry list and upper bounds (CAP / 2 each)
+    return 3 * CAP * sizeof(uint32_t);
 }
 
 template <int THREADS, uint32_t CAP>
-void set_cta_attr() {
-    if (cta_smem<THREADS, CAP>() > 48 * 1024)
-        CK(cudaFuncSetAttribute((const void *)k_improve_cta<THREADS, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)cta_smem<THREADS, CAP>()));
+void set_cta_attr() {   // always: dynamic plus static shared memory may pass 48 KB
+    CK(cudaFuncSetAttribute((const void *)k_improve_cta<THREADS, CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)cta_smem<THREADS, CAP>()));
 }
 
 }  // namespace
