@@ -259,7 +259,7 @@ void Ctx::free_all() {
     b = Batch();
     big_tables = nullptr;
     pin64 = nullptr;
-    pin32 = nullptr;
+    civ = nullptr;
     num_comms = 0;
 }
 
@@ -355,7 +355,7 @@ void finish_graph(Ctx &c) {
         c.st[k].intl = c.alloc<int32_t>(n);
     }
     c.pin64 = c.alloc<double>(n);
-    c.pin32 = c.alloc<float2>(n);
+    c.civ = c.alloc<int4>(n);
     c.slot_flag = c.alloc<uint8_t>(2 * (size_t)g.m);
     c.itcount = c.alloc<uint32_t>(n);
     c.itdeg = c.alloc<int32_t>(n);

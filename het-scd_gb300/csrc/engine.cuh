@@ -200,7 +200,7 @@ struct Ctx {
     uint32_t *host_u32 = nullptr;     // pinned: the active-graph count of an iteration
     uint32_t *big_tables = nullptr;   // global hash tables of the last degree bucket
     double *pin64 = nullptr;          // per-community p_in of the current statistics
-    float2 *pin32 = nullptr;          // and its FP32 enclosure
+    int4 *civ = nullptr;              // size, external edges and the FP32 enclosure of p_in (bits)
     uint32_t *work_counter = nullptr; // dynamic work distribution
 
     PhaseTimers timers;

@@ -35,7 +35,7 @@ struct ImproveArgs {
     const uint32_t *indices, *adj, *labels;
     Stats st;
     const double *pin64;   // p_in of every community (src/scd.cpp:296-298)
-    const float2 *pin32;   // its FP32 enclosure
+    const int4 *civ;       // per label: size, external edges, FP32 enclosure of p_in (bits)
     const double *p_ext;      // per graph
     const float2 *pe32;       // per graph: FP32 enclosure of p_ext
     const uint32_t *gid;      // graph of each vertex (nullptr: one graph)
@@ -72,20 +72,14 @@ __device__ __forceinline__ double exact_gain(const ImproveArgs &a, uint32_t l, u
     return wcc_gain(size, (int)freq, (int)deg - (int)freq, ext, p_in, p_ext, a.alpha);
 }
 
-__device__ __forceinline__ Iv interval_gain(const ImproveArgs &a, uint32_t l, uint32_t freq, uint32_t deg,
-                                            Iv p_ext, Iv alpha, bool *exact_needed) {
-    const float2 pin = a.pin32[l];
-    return wcc_gain_iv(a.st.sizes[l], (int)freq, (int)deg - (int)freq, a.st.ext[l], Iv{pin.x, pin.y}, p_ext, alpha,
-                       exact_needed);
-}
-
 // Interval of the gain of label l, own label included (the negated remove gain:
 // the community without p, as exact_gain's l == mine branch, with
 // community_p_in enclosed).  One wcc_gain_iv call for both kinds, so lanes of a
 // warp holding own and foreign labels do not diverge through it.
 __device__ __forceinline__ Iv interval_any_gain(const ImproveArgs &a, uint32_t l, bool own, uint32_t freq,
                                                 uint32_t deg, Iv p_ext, Iv alpha, bool *exact_needed) {
-    int size = a.st.sizes[l], ext = a.st.ext[l];
+    const int4 cv = a.civ[l];   // one 16-byte read: size, external edges, p_in enclosure
+    int size = cv.x, ext = cv.y;
     Iv pin;
     bool pin_bad = false;
     if (own) {
@@ -94,8 +88,7 @@ __device__ __forceinline__ Iv interval_any_gain(const ImproveArgs &a, uint32_t l
         const int in = a.st.intl[l] / 2 - (int)freq;
         pin = size > 1 ? iv_div(iv_int(2 * in), iv_mul(iv_int(size), iv_int(size - 1)), &pin_bad) : Iv{0.f, 0.f};
     } else {
-        const float2 p = a.pin32[l];
-        pin = Iv{p.x, p.y};
+        pin = Iv{__int_as_float(cv.z), __int_as_float(cv.w)};
     }
     const Iv g = wcc_gain_iv(size, (int)freq, (int)deg - (int)freq, ext, pin, p_ext, alpha, exact_needed);
     *exact_needed = *exact_needed || pin_bad;
@@ -132,11 +125,12 @@ __device__ __forceinline__ uint32_t decide(double best_gain, uint32_t best_label
     return mine;
 }
 
-__global__ void k_comm_prep(uint32_t nc, Stats st, double *pin64, float2 *pin32) {
+__global__ void k_comm_prep(uint32_t nc, Stats st, double *pin64, int4 *civ) {
     for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < nc; l += gridDim.x * blockDim.x) {
         const double p = community_p_in(st.sizes[l], st.intl[l] / 2);
         pin64[l] = p;
-        pin32[l] = make_float2(__double2float_rd(p), __double2float_ru(p));
+        civ[l] = make_int4(st.sizes[l], st.ext[l], __float_as_int(__double2float_rd(p)),
+                           __float_as_int(__double2float_ru(p)));
     }
 }
 
@@ -766,11 +760,11 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
     PhaseScope ph(c, "improve");
     prepare_improve_kernels();
     if (c.num_comms) {
-        k_comm_prep<<<grid_for(c.num_comms, TPB), TPB, 0, s>>>(c.num_comms, st, c.pin64, c.pin32);
+        k_comm_prep<<<grid_for(c.num_comms, TPB), TPB, 0, s>>>(c.num_comms, st, c.pin64, c.civ);
         CK_LAUNCH("k_comm_prep");
         c.launches++;
     }
-    ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.pin32, c.b.p_ext, c.b.pe32, c.b.gid,
+    ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.civ, c.b.p_ext, c.b.pe32, c.b.gid,
                   frozen_graphs ? c.b.active : nullptr, c.alpha, next};
     const DegreeClasses &k = g.cls;
     if (k.count[0]) {
