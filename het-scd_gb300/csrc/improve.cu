@@ -538,7 +538,9 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     __shared__ uint32_t s_n;
     __shared__ int s_need;        // some foreign interval was not usable
     __shared__ int s_own;         // 0 no own label among the neighbours, 1 sign known, 2 exact needed
-    __shared__ float s_own_hi;
+    __shared__ float s_own_lo, s_own_hi;
+    __shared__ float s_mhi[THREADS / 32];
+    __shared__ uint32_t s_mlab[THREADS / 32], s_surv[THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t beg = a.indices[p], deg = a.indices[p + 1] - beg, mine = a.labels[p];
     const uint32_t mask = cap - 1;
@@ -591,13 +593,15 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     const uint32_t nl = s_n;
     // pass 1: best lower and upper bounds among foreign labels, the own label's
     // interval; hi_of[i] keeps label i's upper bound for pass 2 (+inf: unusable)
-    float m = -INFINITY, mh = -INFINITY;
+    float m = -INFINITY, mh = -INFINITY, m_hi = -INFINITY;   // m_hi: upper bound of the label holding m
+    uint32_t m_label = INVALID;
     for (uint32_t i = threadIdx.x; i < nl; i += THREADS) {
         const uint32_t h = list[i], l = keys[h];
         bool need = false;
         const Iv iv = interval_any_gain(a, l, l == mine, vals[h], deg, pe, al, &need);
         if (l == mine) {
             s_own = own_sign_known(iv, need) ? 1 : 2;
+            s_own_lo = iv.lo;
             s_own_hi = iv.hi;
             hi_of[i] = -INFINITY;
             continue;
@@ -606,31 +610,72 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
             s_need = 1;
             hi_of[i] = INFINITY;
         } else {
-            m = fmaxf(m, iv.lo);
+            if (iv.lo > m || (iv.lo == m && l < m_label)) {
+                m = iv.lo;
+                m_hi = iv.hi;
+                m_label = l;
+            }
             mh = fmaxf(mh, iv.hi);
             hi_of[i] = iv.hi;
         }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        m = fmaxf(m, __shfl_xor_sync(FULL, m, o));
+        const float om = __shfl_xor_sync(FULL, m, o), omh = __shfl_xor_sync(FULL, m_hi, o);
+        const uint32_t oml = __shfl_xor_sync(FULL, m_label, o);
+        if (om > m || (om == m && oml < m_label)) {
+            m = om;
+            m_hi = omh;
+            m_label = oml;
+        }
         mh = fmaxf(mh, __shfl_xor_sync(FULL, mh, o));
     }
     if (lane == 0) {
         s_lo[warp] = m;
         s_hi[warp] = mh;
+        s_mhi[warp] = m_hi;
+        s_mlab[warp] = m_label;
     }
     __syncthreads();
     m = s_lo[0];
     mh = s_hi[0];
+    m_hi = s_mhi[0];
+    m_label = s_mlab[0];
 #pragma unroll
     for (int w = 1; w < THREADS / 32; w++) {
-        m = fmaxf(m, s_lo[w]);
+        if (s_lo[w] > m || (s_lo[w] == m && s_mlab[w] < m_label)) {
+            m = s_lo[w];
+            m_hi = s_mhi[w];
+            m_label = s_mlab[w];
+        }
         mh = fmaxf(mh, s_hi[w]);
     }
     // a foreign label survives iff its interval is unusable or hi > 0 and hi >= m;
     // the one with the largest hi decides whether any does
     const bool any_survivor = s_need || (mh > 0.f && mh >= m);
+    // the intervals alone decide when the label holding m > 0 is the only survivor
+    // and the own label's interval is usable (decide_iv); no exact gain is then needed
+    if (!s_need && m > 0.f && s_own != 2) {
+        uint32_t surv = 0;
+        for (uint32_t i0 = 0; i0 < nl; i0 += THREADS) {
+            const uint32_t i = i0 + threadIdx.x;
+            const float hi = i < nl ? hi_of[i] : -INFINITY;
+            surv += __popc(__ballot_sync(FULL, hi > 0.f && hi >= m));
+        }
+        if (lane == 0) s_surv[warp] = surv;
+        __syncthreads();
+        surv = 0;
+#pragma unroll
+        for (int w = 0; w < THREADS / 32; w++) surv += s_surv[w];
+        if (surv == 1) {
+            const uint32_t dec = decide_iv(Iv{m, m_hi}, m_label, s_own != 0, Iv{s_own_lo, s_own_hi}, mine);
+            if (dec != UNDECIDED) {
+                if (threadIdx.x == 0) a.next[p] = dec;
+                __syncthreads();
+                return;
+            }
+        }
+    }
     // pass 2: exact gains of the survivors and, if needed, of the own label (remove gain)
     double bg = 0.0;
     uint32_t bl = INVALID;
