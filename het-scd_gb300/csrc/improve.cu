@@ -539,6 +539,7 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     __shared__ int s_need;        // some foreign interval was not usable
     __shared__ int s_own;         // 0 no own label among the neighbours, 1 sign known, 2 exact needed
     __shared__ float s_own_lo, s_own_hi;
+    __shared__ uint32_t s_own_i;  // the own label's position in the entry list
     __shared__ float s_mhi[THREADS / 32];
     __shared__ uint32_t s_mlab[THREADS / 32], s_surv[THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -603,6 +604,7 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
             s_own = own_sign_known(iv, need) ? 1 : 2;
             s_own_lo = iv.lo;
             s_own_hi = iv.hi;
+            s_own_i = i;
             hi_of[i] = -INFINITY;
             continue;
         }
@@ -679,15 +681,15 @@ __device__ void improve_cta(const ImproveArgs &a, uint32_t p, uint32_t *keys, ui
     // pass 2: exact gains of the survivors and, if needed, of the own label (remove gain)
     double bg = 0.0;
     uint32_t bl = INVALID;
+    if (s_own && threadIdx.x == (s_own_i & (THREADS - 1))) {   // the own label (remove gain)
+        const uint32_t h = list[s_own_i];
+        if (any_survivor || s_own == 2) s_remove = -exact_gain(a, mine, vals[h], deg, mine, p_ext);
+        else if (s_own_hi < 0.f) s_remove = 1.0;   // only its sign matters when nothing survives
+    }
     for (uint32_t i = threadIdx.x; i < nl; i += THREADS) {
-        const uint32_t h = list[i], l = keys[h];
-        if (l == mine) {
-            if (any_survivor || s_own == 2) s_remove = -exact_gain(a, l, vals[h], deg, mine, p_ext);
-            else if (s_own_hi < 0.f) s_remove = 1.0;   // only its sign matters when nothing survives
-            continue;
-        }
-        const float hi = hi_of[i];
+        const float hi = hi_of[i];   // -inf for the own label
         if (hi > 0.f && hi >= m) {
+            const uint32_t h = list[i], l = keys[h];
             const double g = exact_gain(a, l, vals[h], deg, mine, p_ext);
             if (g > 0.0 && (bl == INVALID || better(g, l, bg, bl))) {
                 bg = g;
