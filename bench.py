@@ -229,7 +229,8 @@ def bench_batched(S, device, args):
     groups = split_batches(sizes, args.batch_records)
     eng = S.Engine(device)
     eng.batch_convert([graphs[i] for i in groups[0]])
-    tune = eng.autotune() if not args.no_autotune else {"small_max": None, "warp_max": None, "cta_max": None}
+    tune = eng.autotune() if not args.no_autotune else {"small_max": None, "warp_max": None, "cta_max": None,
+                                                         "in_list_min": None}
 
     def run_group(ids):
         eng.batch_convert([graphs[i] for i in ids])
@@ -285,7 +286,8 @@ def bench_batched(S, device, args):
             "per_graph_loop": {"graphs_per_s": l_gps, "edges_per_s": loop_records / loop_s, "sample_graphs": len(sample),
                                "seconds": loop_s},
             "speedup_vs_loop": b_gps / l_gps, "identical_on_sample": bool(same),
-            "autotune": {"small_max": tune["small_max"], "warp_max": tune["warp_max"], "cta_max": tune["cta_max"]},
+            "autotune": {"small_max": tune["small_max"], "warp_max": tune["warp_max"], "cta_max": tune["cta_max"],
+                         "in_list_min": tune["in_list_min"]},
             "timing": "host wall clock, host edge lists in, host labels out", "generate_s": round(gen_s, 1)}
 
 

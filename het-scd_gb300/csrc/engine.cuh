@@ -136,7 +136,8 @@ struct TcPlan {
     uint32_t *unit_off[K] = {};
     uint32_t nverts[K] = {};
     uint32_t nfwd[K] = {};
-    uint32_t dir_lo = 0, dir_hi = 0;   // b-centric iff d+(a) < d+(b) and dir_lo < d+(b) <= dir_hi
+    uint32_t dir_lo = 0, dir_hi = 0, dir_amin = 0;   // b-centric iff d+(a) < d+(b),
+                                                      // dir_lo < d+(b) <= dir_hi, d+(a) > dir_amin
     DevBuf<uint32_t> tmp[2 * K];   // storage when the plan is temporary
 };
 struct Ctx;
@@ -177,6 +178,7 @@ struct Ctx {
     std::string err;
     uint64_t launches = 0;
     uint32_t tc_small = 32, tc_b0 = 64, tc_b1 = 1024;   // triangle-counting bucket splits (autotuned)
+    uint32_t tc_amin = 0;   // b-centric edges need d+(a) > tc_amin (autotuned; at most tc_small)
 
     Graph g;
     Batch b;

@@ -46,10 +46,15 @@ constexpr int ITEMS = 8;   // consecutive items per thread
 
 constexpr uint32_t HASH_MUL = 0x9E3779B1u;   // multiplicative hash: table index = top bits
 
-// a -> b (d+(a), d+(b)) is counted at b's table iff d+(a) < d+(b) and lo < d+(b) <= hi
+// a -> b (d+(a), d+(b)) is counted at b's table iff d+(a) < d+(b), lo < d+(b) <= hi
+// and d+(a) > amin (amin > 0 keeps short out-lists with the register-group kernel,
+// whose binary searches make a long out(b) cheap; which is faster depends on the
+// graph, so amin is one of the autotuned splits)
 struct Dir {
-    uint32_t lo, hi;
-    __device__ __forceinline__ bool bcentric(uint32_t da, uint32_t db) const { return da < db && db > lo && db <= hi; }
+    uint32_t lo, hi, amin;
+    __device__ __forceinline__ bool bcentric(uint32_t da, uint32_t db) const {
+        return da < db && da > amin && db > lo && db <= hi;
+    }
 };
 
 // units of the centres verts[i]: out-list centres (i < nfwd) have d+ partners, in-list centres their in-degree
@@ -504,8 +509,8 @@ void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, LabelFilter lab
                    uint8_t *flag, uint32_t *ctr, unsigned grid, cudaStream_t s) {
     const size_t smem = tc_cta_smem<TCAP, LCAP, FBITS>();
     k_tc_cta<THREADS, ROUNDS, TCAP, LCAP, FBITS, MIN_CTAS><<<grid, THREADS, smem, s>>>(
-        o, plan.verts[k], plan.unit_off[k], plan.nverts[k], plan.nfwd[k], Dir{plan.dir_lo, plan.dir_hi}, labels,
-        tcount, flag, ctr);
+        o, plan.verts[k], plan.unit_off[k], plan.nverts[k], plan.nfwd[k], Dir{plan.dir_lo, plan.dir_hi, plan.dir_amin},
+        labels, tcount, flag, ctr);
     CK_LAUNCH("k_tc_cta");
 }
 
@@ -566,6 +571,7 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
     const bool split = in_lists && !(c.flags & SCD_FLAG_TC_OUT_ONLY);
     plan.dir_lo = split ? b0 : 0;
     plan.dir_hi = split ? B2 : 0;
+    plan.dir_amin = c.tc_amin < sm ? c.tc_amin : sm;
     for (int k = 0; k < TcPlan::K; k++) {
         const bool cta = k == 3 || k == 4;
         const InBucket fa{o, bounds[k], bounds[k + 1], false}, fb{o, bounds[k], bounds[k + 1], true};
@@ -622,47 +628,53 @@ double autotune_tc(Ctx &c, std::vector<std::string> *report) {
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    const uint32_t sms[] = {0, 16, 32}, b0s[] = {16, 32, 64}, b1s[] = {256, 512, 1024};
+    const uint32_t sms[] = {0, 16, 32}, b0s[] = {16, 32, 64}, b1s[] = {256, 512, 1024}, amins[] = {0, 16, 32};
     double best = 1e300;
-    uint32_t best_s = c.tc_small, best0 = c.tc_b0, best1 = c.tc_b1;
+    uint32_t best_s = c.tc_small, best0 = c.tc_b0, best1 = c.tc_b1, best_a = c.tc_amin;
     for (uint32_t sm : sms)
         for (uint32_t b0 : b0s)
-            for (uint32_t b1 : b1s) {
-                if (b0 < sm) continue;   // (S, B0] would be empty: same plan as B0 = S
-                c.tc_small = sm;
-                c.tc_b0 = b0;
-                c.tc_b1 = b1;
-                TcPlan plan;
-                tc_plan(c, o, plan, s, false, true);
-                double ms_min = 1e300;
-                for (int rep = 0; rep < 2; rep++) {
-                    CK(cudaMemsetAsync(tcount.get(), 0, (size_t)g.n * 4, s));
-                    CK(cudaMemsetAsync(flag.get(), 0, 2 * (size_t)g.m, s));
-                    CK(cudaEventRecord(e0, s));
-                    count_triangles(c, o, plan, LabelFilter{}, tcount.get(), flag.get(), s);
-                    CK(cudaEventRecord(e1, s));
-                    CK(cudaEventSynchronize(e1));
-                    float ms = 0;
-                    CK(cudaEventElapsedTime(&ms, e0, e1));
-                    ms_min = ms < ms_min ? ms : ms_min;
+            for (uint32_t b1 : b1s)
+                for (uint32_t am : amins) {
+                    if (b0 < sm) continue;   // (S, B0] would be empty: same plan as B0 = S
+                    if (am > sm) continue;   // same plan as am = S
+                    c.tc_small = sm;
+                    c.tc_b0 = b0;
+                    c.tc_b1 = b1;
+                    c.tc_amin = am;
+                    TcPlan plan;
+                    tc_plan(c, o, plan, s, false, true);
+                    double ms_min = 1e300;
+                    for (int rep = 0; rep < 2; rep++) {
+                        CK(cudaMemsetAsync(tcount.get(), 0, (size_t)g.n * 4, s));
+                        CK(cudaMemsetAsync(flag.get(), 0, 2 * (size_t)g.m, s));
+                        CK(cudaEventRecord(e0, s));
+                        count_triangles(c, o, plan, LabelFilter{}, tcount.get(), flag.get(), s);
+                        CK(cudaEventRecord(e1, s));
+                        CK(cudaEventSynchronize(e1));
+                        float ms = 0;
+                        CK(cudaEventElapsedTime(&ms, e0, e1));
+                        ms_min = ms < ms_min ? ms : ms_min;
+                    }
+                    if (report) {
+                        char buf[112];
+                        snprintf(buf, sizeof buf, "small<=%u warp<=%u cta<=%u in-list>%u: %.3f ms", sm, b0, b1, am,
+                                 ms_min);
+                        report->push_back(buf);
+                    }
+                    if (ms_min < best) {
+                        best = ms_min;
+                        best_s = sm;
+                        best0 = b0;
+                        best1 = b1;
+                        best_a = am;
+                    }
                 }
-                if (report) {
-                    char buf[96];
-                    snprintf(buf, sizeof buf, "small<=%u warp<=%u cta<=%u: %.3f ms", sm, b0, b1, ms_min);
-                    report->push_back(buf);
-                }
-                if (ms_min < best) {
-                    best = ms_min;
-                    best_s = sm;
-                    best0 = b0;
-                    best1 = b1;
-                }
-            }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c.tc_small = best_s;
     c.tc_b0 = best0;
     c.tc_b1 = best1;
+    c.tc_amin = best_a;
     return best;
 }
 
@@ -673,7 +685,7 @@ void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter 
     prepare_tc_kernels();
     uint32_t *ctr = c.work_counter;
     CK(cudaMemsetAsync(ctr, 0, 16, s));
-    const Dir dir{plan.dir_lo, plan.dir_hi};
+    const Dir dir{plan.dir_lo, plan.dir_hi, plan.dir_amin};
     if (plan.nverts[0]) {
         k_tc_small<16><<<grid_for((uint64_t)plan.nverts[0] * 16, 256, 152 * 8), 256, 0, s>>>(
             o, plan.verts[0], plan.nverts[0], dir, labels, tcount, flag);

@@ -305,8 +305,14 @@ class Engine:
         buf = ctypes.create_string_buffer(8192)
         self._check(lib().scd_autotune(self._ctx, ctypes.byref(sm), ctypes.byref(w), ctypes.byref(c),
                                        ctypes.byref(ms), buf, 8192))
-        return dict(small_max=sm.value, warp_max=w.value, cta_max=c.value, best_ms=ms.value,
-                    report=buf.value.decode().splitlines())
+        report = buf.value.decode().splitlines()
+        # the in-list split is not an ABI output: it is in the report line of the chosen split
+        chosen = f"small<={sm.value} warp<={w.value} cta<={c.value} in-list>"
+        best = min((ln for ln in report if ln.startswith(chosen)), default=None,
+                   key=lambda ln: float(ln.rsplit(":", 1)[1].split()[0]))
+        in_list_min = int(best[len(chosen):].split(":")[0]) if best else None
+        return dict(small_max=sm.value, warp_max=w.value, cta_max=c.value, in_list_min=in_list_min,
+                    best_ms=ms.value, report=report)
 
     def stream(self):
         p = ctypes.c_void_p()

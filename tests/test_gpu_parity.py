@@ -236,3 +236,23 @@ def test_in_list_units_agree_with_out_list_counting(engine, make):
         assert np.array_equal(engine.labels_from_device(), e2.labels_from_device())
     finally:
         e2.close()
+
+
+def test_autotune_keeps_results():
+    # every split the autotuner may pick counts the same triangles
+    pairs = scdgen.chunglu(40_000, 2.1, 5.0, 3000.0, 0.2, 10, 200, seed=9)
+    e = S.Engine(0)
+    try:
+        e.convert_edges(pairs)
+        ref = e.graph_bytes()
+        r0 = e.run(0.01, 20)
+        t = e.autotune()
+        assert t["small_max"] in (0, 16, 32) and t["warp_max"] in (16, 32, 64) and t["cta_max"] in (256, 512, 1024)
+        assert t["in_list_min"] in (0, 16, 32) and t["in_list_min"] <= t["small_max"]
+        assert len(t["report"]) > 20
+        e.convert_edges(pairs)
+        assert e.graph_bytes() == ref
+        r1 = e.run(0.01, 20)
+        assert r1["wcc"] == r0["wcc"]
+    finally:
+        e.close()
