@@ -57,6 +57,10 @@ __global__ void k_positions(uint32_t n, const uint32_t *__restrict__ order, uint
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) pos[order[i]] = i;
 }
 
+// vertices of degree > HUB_DEG are scanned by a whole CTA (k_mis_round_hub, k_claim_hub):
+// a hub has thousands of earlier neighbours, one warp would walk them one load chain at a time
+constexpr uint32_t HUB_DEG = 4096, HUB_TPB = 1024;
+
 __global__ void __launch_bounds__(TPB)
 k_mis_round(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ adj,
             const uint32_t *__restrict__ pos, uint8_t *state, uint32_t *undecided) {
@@ -64,6 +68,7 @@ k_mis_round(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__
     for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += (gridDim.x * blockDim.x) >> 5) {
         if (((volatile uint8_t *)state)[v] != UNDECIDED) continue;
         const uint32_t pv = pos[v], beg = indices[v], deg = indices[v + 1] - beg;
+        if (deg > HUB_DEG) continue;
         bool seed_seen = false, open = false;
         for (uint32_t i0 = 0; i0 < deg && !seed_seen; i0 += 32) {
             bool s = false, u = false;
@@ -86,6 +91,39 @@ k_mis_round(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__
     }
 }
 
+// the same round for the hubs (list hubs[count], all of degree > HUB_DEG), one CTA each
+__global__ void __launch_bounds__(HUB_TPB)
+k_mis_round_hub(const uint32_t *__restrict__ hubs, uint32_t count, const uint32_t *__restrict__ indices,
+                const uint32_t *__restrict__ adj, const uint32_t *__restrict__ pos, uint8_t *state,
+                uint32_t *undecided) {
+    for (uint32_t h = blockIdx.x; h < count; h += gridDim.x) {
+        const uint32_t v = hubs[h];
+        if (((volatile uint8_t *)state)[v] != UNDECIDED) continue;   // CTA-uniform
+        const uint32_t pv = pos[v], beg = indices[v], deg = indices[v + 1] - beg;
+        int seed_seen = 0, open = 0;
+        for (uint32_t i0 = 0; i0 < deg && !seed_seen; i0 += HUB_TPB) {
+            bool s = false, u = false;
+            const uint32_t i = i0 + threadIdx.x;
+            if (i < deg) {
+                const uint32_t w = adj[beg + i];
+                if (pos[w] < pv) {
+                    const uint8_t st = ((volatile uint8_t *)state)[w];
+                    s = st == SEED;
+                    u = st == UNDECIDED;
+                }
+            }
+            seed_seen = __syncthreads_or(s);
+            open = __syncthreads_or(u) || open;
+        }
+        if (threadIdx.x == 0) {
+            if (seed_seen) state[v] = NONSEED;
+            else if (!open) state[v] = SEED;
+            else atomicAdd(undecided, 1u);
+        }
+        __syncthreads();
+    }
+}
+
 struct SeedAt {
     const uint32_t *order;
     const uint8_t *state;
@@ -105,6 +143,7 @@ k_claim_labels(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t 
     for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += (gridDim.x * blockDim.x) >> 5) {
         if (state[v] != NONSEED) continue;
         const uint32_t beg = indices[v], deg = indices[v + 1] - beg;
+        if (deg > HUB_DEG) continue;
         uint32_t best_pos = INVALID, best = INVALID;
         for (uint32_t i = lane; i < deg; i += 32) {
             const uint32_t w = adj[beg + i];
@@ -122,6 +161,33 @@ k_claim_labels(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t 
             }
         }
         if (lane == 0) labels[v] = labels[best];
+    }
+}
+
+// the earliest seed neighbour of a non-seed hub, one CTA per hub
+__global__ void __launch_bounds__(HUB_TPB)
+k_claim_hub(const uint32_t *__restrict__ hubs, uint32_t count, const uint32_t *__restrict__ indices,
+            const uint32_t *__restrict__ adj, const uint32_t *__restrict__ pos, const uint8_t *__restrict__ state,
+            uint32_t *labels) {
+    __shared__ unsigned long long s_best;
+    for (uint32_t h = blockIdx.x; h < count; h += gridDim.x) {
+        const uint32_t v = hubs[h];
+        if (state[v] != NONSEED) continue;   // CTA-uniform
+        if (threadIdx.x == 0) s_best = ~0ull;
+        __syncthreads();
+        const uint32_t beg = indices[v], deg = indices[v + 1] - beg;
+        unsigned long long best = ~0ull;   // (position, vertex) of the earliest seed neighbour
+        for (uint32_t i = threadIdx.x; i < deg; i += HUB_TPB) {
+            const uint32_t w = adj[beg + i];
+            if (state[w] == SEED) {
+                const unsigned long long key = ((unsigned long long)pos[w] << 32) | w;
+                best = key < best ? key : best;
+            }
+        }
+        if (best != ~0ull) atomicMin(&s_best, best);
+        __syncthreads();
+        if (threadIdx.x == 0) labels[v] = labels[(uint32_t)s_best];
+        __syncthreads();
     }
 }
 
@@ -161,8 +227,17 @@ void initial_partition(Ctx &c) {
     DevBuf<uint8_t> state(n, s);
     CK(cudaMemsetAsync(state.get(), UNDECIDED, n, s));
     const unsigned G = grid_for((uint64_t)n * 32, TPB);
+    const uint32_t *hubs = g.cls.list[DegreeClasses::K - 1];   // degree > 4096 = HUB_DEG
+    const uint32_t nhubs = g.cls.count[DegreeClasses::K - 1];
+    static_assert(DegreeClasses::upper[DegreeClasses::K - 2] == HUB_DEG, "hub class");
     for (int round = 0;; round++) {
         CK(cudaMemsetAsync(undecided.get(), 0, 4, s));
+        if (nhubs) {
+            k_mis_round_hub<<<grid_for(nhubs, 1, 152 * 2), HUB_TPB, 0, s>>>(hubs, nhubs, g.indices, g.adj, pos.get(),
+                                                                         state.get(), undecided.get());
+            CK_LAUNCH("k_mis_round_hub");
+            c.launches++;
+        }
         k_mis_round<<<G, TPB, 0, s>>>(n, g.indices, g.adj, pos.get(), state.get(), undecided.get());
         CK_LAUNCH("k_mis_round");
         c.launches++;
@@ -179,6 +254,12 @@ void initial_partition(Ctx &c) {
     CK_LAUNCH("k_seed_labels");
     k_claim_labels<<<G, TPB, 0, s>>>(n, g.indices, g.adj, pos.get(), state.get(), c.labels);
     CK_LAUNCH("k_claim_labels");
+    if (nhubs) {
+        k_claim_hub<<<grid_for(nhubs, 1, 152 * 2), HUB_TPB, 0, s>>>(hubs, nhubs, g.indices, g.adj, pos.get(),
+                                                                 state.get(), c.labels);
+        CK_LAUNCH("k_claim_hub");
+        c.launches++;
+    }
     c.launches += 4;
     k_comm_off<<<grid_for(c.b.G + 1, TPB), TPB, 0, s>>>(c.b.G, c.b.fin_off, rank.get(), c.b.comm_off);
     CK_LAUNCH("k_comm_off");
