@@ -1,7 +1,9 @@
 // Context management, per-graph setup and the C ABI (include/scd_gb300.h).
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <new>
 
 #include "engine.cuh"
@@ -641,6 +643,10 @@ void scd_destroy(scd_ctx *ctx) {
     if (c.work_counter) cudaFree(c.work_counter);
     if (c.wcc_host) cudaFreeHost(c.wcc_host);
     if (c.host_u32) cudaFreeHost(c.host_u32);
+    for (int k = 0; k < 2; k++) {
+        if (c.io_buf[k]) cudaFreeHost(c.io_buf[k]);
+        if (c.io_done[k]) cudaEventDestroy(c.io_done[k]);
+    }
     c.timers.destroy();
     if (c.pext_ready) cudaEventDestroy(c.pext_ready);
     if (c.stream) cudaStreamDestroy(c.stream);
@@ -672,6 +678,100 @@ int scd_transfer_graph(scd_ctx *ctx, uint32_t n, uint32_t m, const uint32_t *ind
         c.alpha = alpha;
         upload_graph(c, n, m, indices, adj, tri, tri_deg);
         CK(cudaStreamSynchronize(c.stream));
+    });
+}
+
+namespace {
+
+constexpr size_t IO_PIECE = 64u << 20;   // bytes per pinned piece of a graph file
+
+// Piece [off, off + len) of a graph file's body (everything after the two header
+// words) to the resident graph's arrays: the body is indices | adj | tri | tri_deg.
+void body_to_device(Ctx &c, const char *src, uint64_t off, uint64_t len) {
+    const Graph &g = c.g;
+    const uint64_t seg_len[4] = {4 * ((uint64_t)g.n + 1), 8 * (uint64_t)g.m, 4 * (uint64_t)g.n, 4 * (uint64_t)g.n};
+    char *seg_dst[4] = {(char *)g.indices, (char *)g.adj, (char *)g.tri, (char *)g.tri_deg};
+    uint64_t seg_beg = 0;
+    for (int k = 0; k < 4; k++) {
+        const uint64_t a = off > seg_beg ? off : seg_beg, e = seg_beg + seg_len[k];
+        const uint64_t b = off + len < e ? off + len : e;
+        if (a < b) CK(cudaMemcpyAsync(seg_dst[k] + (a - seg_beg), src + (a - off), b - a, cudaMemcpyHostToDevice, c.stream));
+        seg_beg = e;
+    }
+}
+
+// the body is on the device: check its offsets, then the derived arrays
+void finish_loaded_graph(Ctx &c, double alpha) {
+    uint32_t ends[2] = {0, 0};
+    CK(cudaMemcpyAsync(ends, c.g.indices, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaMemcpyAsync(ends + 1, c.g.indices + c.g.n, 4, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (ends[0] != 0 || ends[1] != 2 * (uint64_t)c.g.m) {
+        c.free_all();
+        throw Error(SCD_ERR_FORMAT, "indices do not match m");
+    }
+    c.alpha = alpha;
+    c.has_graph = true;
+    finish_graph(c);
+    CK(cudaStreamSynchronize(c.stream));
+}
+
+uint64_t graph_file_bytes(uint32_t n, uint32_t m) { return 4 * (2 + ((uint64_t)n + 1) + 2 * (uint64_t)m + 2 * (uint64_t)n); }
+
+}  // namespace
+
+int scd_transfer_graph_bytes(scd_ctx *ctx, const void *bytes, uint64_t size, double alpha) {
+    return guarded(ctx, [&](Ctx &c) {
+        if (!bytes || size < 8) throw Error(SCD_ERR_ARG, "no graph bytes");
+        uint32_t hdr[2];
+        memcpy(hdr, bytes, 8);
+        if (graph_file_bytes(hdr[0], hdr[1]) != size) throw Error(SCD_ERR_FORMAT, "graph size does not match n and m");
+        alloc_graph(c, hdr[0], hdr[1]);
+        body_to_device(c, (const char *)bytes + 8, 0, size - 8);
+        finish_loaded_graph(c, alpha);
+    });
+}
+
+// Read in IO_PIECE pieces into two pinned buffers: the read of one piece overlaps
+// the copy of the other; no pageable host copy of the graph is made.
+int scd_load_graph_file(scd_ctx *ctx, const char *path, double alpha) {
+    return guarded(ctx, [&](Ctx &c) {
+        if (!path) throw Error(SCD_ERR_ARG, "NULL path");
+        FILE *f = fopen(path, "rb");
+        if (!f) throw Error(SCD_ERR_ARG, std::string("failed to open ") + path);
+        struct Closer {
+            FILE *f;
+            ~Closer() { fclose(f); }
+        } closer{f};
+        const std::string bad = std::string("error while reading ") + path;
+        uint32_t hdr[2];
+        if (fread(hdr, 4, 2, f) != 2) throw Error(SCD_ERR_FORMAT, bad);
+        if (fseek(f, 0, SEEK_END) != 0) throw Error(SCD_ERR_FORMAT, bad);
+        const long long fsize = ftell(f);
+        if (fsize < 0 || (uint64_t)fsize != graph_file_bytes(hdr[0], hdr[1]) || fseek(f, 8, SEEK_SET) != 0)
+            throw Error(SCD_ERR_FORMAT, bad);
+        for (int k = 0; k < 2; k++)
+            if (!c.io_buf[k]) {
+                CK(cudaMallocHost((void **)&c.io_buf[k], IO_PIECE));
+                CK(cudaEventCreateWithFlags(&c.io_done[k], cudaEventDisableTiming));
+            }
+        alloc_graph(c, hdr[0], hdr[1]);
+        const uint64_t body = (uint64_t)fsize - 8;
+        bool used[2] = {false, false};
+        int k = 0;
+        for (uint64_t off = 0; off < body; off += IO_PIECE, k ^= 1) {
+            const uint64_t len = body - off < IO_PIECE ? body - off : IO_PIECE;
+            if (used[k]) CK(cudaEventSynchronize(c.io_done[k]));   // its previous piece has left
+            if (fread(c.io_buf[k], 1, len, f) != len) {
+                CK(cudaStreamSynchronize(c.stream));
+                c.free_all();
+                throw Error(SCD_ERR_FORMAT, bad);
+            }
+            body_to_device(c, c.io_buf[k], off, len);
+            CK(cudaEventRecord(c.io_done[k], c.stream));
+            used[k] = true;
+        }
+        finish_loaded_graph(c, alpha);
     });
 }
 

@@ -200,6 +200,8 @@ struct Ctx {
     TcPlan wplan;                     // triangle-counting plan of the resident graph
     double *wcc_part = nullptr, *wcc_host = nullptr;
     uint32_t *host_u32 = nullptr;     // pinned: the active-graph count of an iteration
+    char *io_buf[2] = {};             // pinned pieces of a graph file on its way to the device
+    cudaEvent_t io_done[2] = {};
     uint32_t *big_tables = nullptr;   // global hash tables of the last degree bucket
     double *pin64 = nullptr;          // per-community p_in of the current statistics
     int4 *civ = nullptr;              // size, external edges and the FP32 enclosure of p_in (bits)
@@ -230,6 +232,8 @@ struct Ctx {
 void convert_edges(Ctx &c, const uint32_t *pairs_dev, uint64_t count, const std::vector<uint64_t> *rec_off = nullptr);
 // read_edges on the device: (min, max) records of the text in file order into out
 uint64_t parse_edge_text(Ctx &c, const char *text, uint64_t bytes, DevBuf<uint32_t> &out);
+// empty graph arrays of n vertices and m edges in place of the resident graph
+void alloc_graph(Ctx &c, uint32_t n, uint32_t m);
 void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
                   const int32_t *tri, const int32_t *tri_deg);
 void finish_graph(Ctx &c);   // nlow, p_ext, degree classes, partition buffers

@@ -518,9 +518,7 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     finish_graph(c);
 }
 
-void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
-                  const int32_t *tri, const int32_t *tri_deg) {
-    cudaStream_t s = c.stream;
+void alloc_graph(Ctx &c, uint32_t n, uint32_t m) {
     const uint32_t NG = c.b.G;   // > 1 only for a batch of empty graphs
     c.free_all();
     c.b.G = NG;
@@ -533,6 +531,13 @@ void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const
     g.adj = c.alloc<uint32_t>(2 * (size_t)m);
     g.tri = c.alloc<int32_t>(n);
     g.tri_deg = c.alloc<int32_t>(n);
+}
+
+void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
+                  const int32_t *tri, const int32_t *tri_deg) {
+    cudaStream_t s = c.stream;
+    alloc_graph(c, n, m);
+    Graph &g = c.g;
     if (indices) {
         CK(cudaMemcpyAsync(g.indices, indices, ((size_t)n + 1) * 4, cudaMemcpyHostToDevice, s));
         if (m) CK(cudaMemcpyAsync(g.adj, adj, 2 * (size_t)m * 4, cudaMemcpyHostToDevice, s));

@@ -84,6 +84,8 @@ def lib():
             "scd_batch_labels_all": ([P, P, P], i32),
             "scd_autotune": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(dbl),
                               ctypes.c_char_p, u64], i32),
+            "scd_load_graph_file": ([P, ctypes.c_char_p, dbl], i32),
+            "scd_transfer_graph_bytes": ([P, ctypes.c_char_p, u64, dbl], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -161,6 +163,14 @@ class Engine:
         arrs = [np.ascontiguousarray(getattr(g, k), dtype=t) for k, t in
                 (("indices", np.uint32), ("adj", np.uint32), ("tri", np.int32), ("tri_deg", np.int32))]
         self._check(lib().scd_transfer_graph(self._ctx, g.n, g.m, *[_p(a) for a in arrs], alpha))
+
+    def load_graph_file(self, path, alpha=1.0):
+        """A binary-format graph file straight to the device (pinned pieces)."""
+        self._check(lib().scd_load_graph_file(self._ctx, os.fsencode(path), alpha))
+
+    def transfer_graph_bytes(self, data, alpha=1.0):
+        """A graph file's full contents (bytes) to the device."""
+        self._check(lib().scd_transfer_graph_bytes(self._ctx, bytes(data), len(data), alpha))
 
     def graph_info(self):
         n, m, cc = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_double()

@@ -89,6 +89,18 @@ int scd_transfer_graph(scd_ctx *ctx, uint32_t n, uint32_t m, const uint32_t *ind
                        const uint32_t *adj, const int32_t *tri, const int32_t *tri_deg,
                        double alpha);
 
+/* The binary-format fast path: Graph::read (src/graph.cpp:273-321) and
+ * cuda_transfer_graph in one call.  The file goes to the device in 64 MB pieces
+ * through two pinned buffers (reading one piece overlaps copying the other), with
+ * no pageable host copy of the graph; p_ext on the device.  SCD_ERR_ARG if the
+ * file cannot be opened, SCD_ERR_FORMAT ("error while reading <path>") if it is
+ * short, long or inconsistent. */
+int scd_load_graph_file(scd_ctx *ctx, const char *path, double alpha);
+
+/* The same for a graph file already in host memory (bytes: its full contents;
+ * pinned memory makes the copy asynchronous). */
+int scd_transfer_graph_bytes(scd_ctx *ctx, const void *bytes, uint64_t size, double alpha);
+
 /* Graph sizes and p_ext of the resident graph (src/graph.hpp:25-27). */
 int scd_graph_info(scd_ctx *ctx, uint32_t *n, uint32_t *m, double *clustering_coef);
 

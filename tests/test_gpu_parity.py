@@ -232,7 +232,7 @@ def test_in_list_units_agree_with_out_list_counting(engine, make):
         e2.convert_edges(pairs)
         assert e2.graph_bytes() == engine.graph_bytes()
         r1, r2 = engine.run(0.01, 20), e2.run(0.01, 20)
-        assert r1["wcc"] == r2["wcc"] and r1["iterations"] == r2["iterations"]
+        assert np.array_equal(r1["wcc"], r2["wcc"]) and r1["iterations"] == r2["iterations"]
         assert np.array_equal(engine.labels_from_device(), e2.labels_from_device())
     finally:
         e2.close()
@@ -253,6 +253,6 @@ def test_autotune_keeps_results():
         e.convert_edges(pairs)
         assert e.graph_bytes() == ref
         r1 = e.run(0.01, 20)
-        assert r1["wcc"] == r0["wcc"]
+        assert np.array_equal(r1["wcc"], r0["wcc"])
     finally:
         e.close()
