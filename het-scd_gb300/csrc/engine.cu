@@ -256,6 +256,8 @@ void Ctx::free_all() {
     slot_flag = nullptr;
     itcount = nullptr;
     itdeg = nullptr;
+    int_len = nullptr;
+    int_adj = nullptr;
     wplan = TcPlan();
     wcc_part = nullptr;
     b = Batch();
@@ -361,6 +363,8 @@ void finish_graph(Ctx &c) {
     c.slot_flag = c.alloc<uint8_t>(2 * (size_t)g.m);
     c.itcount = c.alloc<uint32_t>(n);
     c.itdeg = c.alloc<int32_t>(n);
+    c.int_len = c.alloc<uint32_t>(n);
+    c.int_adj = c.alloc<uint32_t>(2 * (size_t)g.m);
     if (n) tc_plan(c, Oriented{g.indices, g.nlow, g.adj, n}, c.wplan, s, true, false);
     c.wcc_part = c.alloc<double>(b.blocks + 1);
     compute_p_ext(c);

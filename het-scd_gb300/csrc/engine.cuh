@@ -151,7 +151,7 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
 void sort_rows(Ctx &c, const uint32_t *off, uint32_t nrows, uint32_t *vals, bool dedup, uint32_t *udeg,
                cudaStream_t s);
 void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter labels, uint32_t *tcount,
-                     uint8_t *flag, cudaStream_t s);
+                     uint8_t *flag, cudaStream_t s, const char *phase = nullptr);
 // times the triangle-counting bucket splits on the resident graph, keeps the fastest
 double autotune_tc(Ctx &c, std::vector<std::string> *report);
 // set kernel attributes (dynamic shared memory) once per device, outside any capture
@@ -197,6 +197,8 @@ struct Ctx {
     uint8_t *slot_flag = nullptr;     // internal-triangle flag per adjacency position
     uint32_t *itcount = nullptr;      // internal triangles per vertex
     int32_t *itdeg = nullptr;         // edges on an internal triangle per vertex
+    uint32_t *int_len = nullptr;      // label-mode count: internal out-list lengths (n)
+    uint32_t *int_adj = nullptr;      // and the internal out-lists at the CSR offsets (2m)
     TcPlan wplan;                     // triangle-counting plan of the resident graph
     double *wcc_part = nullptr, *wcc_host = nullptr;
     uint32_t *host_u32 = nullptr;     // pinned: the active-graph count of an iteration

@@ -452,6 +452,34 @@ void collect_stats(Ctx &c, const uint32_t *labels, Stats &st, bool frozen_graphs
     c.launches++;
 }
 
+// Internal out-lists for the label-mode triangle count: the out-neighbours of v
+// that carry v's (valid) label, in order, at v's CSR offset; length 0 for
+// unlabelled vertices and those of converged graphs.  The internal triangles of
+// compute_wcc (src/wcc.cpp:84-127) are exactly the triangles of this subgraph, so
+// the count walks internal lists only instead of filtering whole out-lists.
+__global__ void __launch_bounds__(TPB)
+k_internal_outlists(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
+                    const uint32_t *__restrict__ adj, LabelFilter lf, uint32_t *ilen, uint32_t *iadj) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += (gridDim.x * blockDim.x) >> 5) {
+        const uint32_t l = lf.labels[v];
+        uint32_t cnt = 0;
+        if (l != INVALID && !lf.frozen(v)) {
+            const uint32_t beg = indices[v], len = nlow[v];
+            for (uint32_t i0 = 0; i0 < len; i0 += 32) {
+                const uint32_t i = i0 + lane;
+                const uint32_t w = i < len ? adj[beg + i] : 0u;
+                const bool keep = i < len && lf.labels[w] == l;
+                const unsigned kb = __ballot_sync(FULL, keep);
+                if (keep) iadj[beg + cnt + __popc(kb & lt)] = w;
+                cnt += __popc(kb);
+            }
+        }
+        if (lane == 0) ilen[v] = cnt;
+    }
+}
+
 void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_graphs) {
     const Graph &g = c.g;
     cudaStream_t s = c.stream;
@@ -463,14 +491,19 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_gra
     CK(cudaMemsetAsync(c.slot_flag, 0, 2 * (size_t)g.m, s));
     CK(cudaMemsetAsync(c.itcount, 0, (size_t)g.n * 4, s));
     CK(cudaMemsetAsync(c.itdeg, 0, (size_t)g.n * 4, s));
-    Oriented o{g.indices, g.nlow, g.adj, g.n};
     const Batch &b = c.b;
     const uint8_t *active = frozen_graphs ? b.active : nullptr;
     const LabelFilter lf{labels, b.gid, active};
-    count_triangles(c, o, c.wplan, lf, c.itcount, c.slot_flag, s);
+    k_internal_outlists<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj, lf, c.int_len,
+                                                                        c.int_adj);
+    CK_LAUNCH("k_internal_outlists");
+    // the plan's buckets (by full out-degree) stay valid: internal lists are never longer
+    const Oriented o{g.indices, c.int_len, c.int_adj, g.n};
+    count_triangles(c, o, c.wplan, LabelFilter{}, c.itcount, c.slot_flag, s, "wcc_tc");
     k_internal_degrees<<<grid_for(((uint64_t)(g.n + 31) / 32 + g.rows.nchunks) * 32, TPB), TPB, 0, s>>>(
-        g.n, g.rows, g.indices, g.nlow, g.adj, c.slot_flag, c.itdeg, lf);
+        g.n, g.rows, g.indices, c.int_len, c.int_adj, c.slot_flag, c.itdeg, lf);
     CK_LAUNCH("k_internal_degrees");
+    c.launches++;
     if (b.blocks) {
         k_wcc_partial<<<b.blocks, TPB, 0, s>>>(b.fin_off, b.blk_off, b.blk_gid, labels, st, g.tri, g.tri_deg,
                                                c.itcount, c.itdeg, c.alpha, c.wcc_part, active);

@@ -679,9 +679,9 @@ double autotune_tc(Ctx &c, std::vector<std::string> *report) {
 }
 
 void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter labels, uint32_t *tcount,
-                     uint8_t *flag, cudaStream_t s) {
+                     uint8_t *flag, cudaStream_t s, const char *phase) {
     if (o.n == 0) return;
-    PhaseScope ph(c, labels.labels ? "wcc_tc" : "tc");
+    PhaseScope ph(c, phase ? phase : labels.labels ? "wcc_tc" : "tc");
     prepare_tc_kernels();
     uint32_t *ctr = c.work_counter;
     CK(cudaMemsetAsync(ctr, 0, 16, s));
