@@ -156,21 +156,27 @@ __global__ void k_max_label(uint32_t n, const uint32_t *__restrict__ labels, uin
     if ((threadIdx.x & 31) == 0) atomicMax(out, m);
 }
 
-uint32_t class_list(Ctx &c, uint32_t lo, uint32_t hi, uint32_t **out) {
+// the vertex lists of K degree ranges (lo[k], hi[k]] with one host read for all counts
+void class_lists(Ctx &c, int K, const uint32_t *lo, const uint32_t *hi, uint32_t **out, uint32_t *cnt) {
     const Graph &g = c.g;
     cudaStream_t s = c.stream;
-    DevBuf<uint32_t> pos((size_t)g.n + 1, s);
-    InClass f{g.indices, lo, hi};
-    scan_exclusive<uint32_t>(f, pos.get(), g.n, s);
-    uint32_t cnt = 0;
-    CK(cudaMemcpyAsync(&cnt, pos.get() + g.n, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    *out = c.alloc<uint32_t>(cnt);
-    if (cnt) {
-        k_class_scatter<<<grid_for(g.n, TPB), TPB, 0, s>>>(g.n, f, pos.get(), *out);
-        CK_LAUNCH("k_class_scatter");
+    std::vector<DevBuf<uint32_t>> pos(K);
+    DevBuf<uint32_t> counts(K, s);
+    for (int k = 0; k < K; k++) {
+        pos[k].alloc((size_t)g.n + 1, s);
+        scan_exclusive<uint32_t>(InClass{g.indices, lo[k], hi[k]}, pos[k].get(), g.n, s);
+        CK(cudaMemcpyAsync(counts.get() + k, pos[k].get() + g.n, 4, cudaMemcpyDeviceToDevice, s));
     }
-    return cnt;
+    CK(cudaMemcpyAsync(cnt, counts.get(), 4 * K, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int k = 0; k < K; k++) {
+        out[k] = c.alloc<uint32_t>(cnt[k]);
+        if (cnt[k]) {
+            k_class_scatter<<<grid_for(g.n, TPB), TPB, 0, s>>>(g.n, InClass{g.indices, lo[k], hi[k]}, pos[k].get(),
+                                                               out[k]);
+            CK_LAUNCH("k_class_scatter");
+        }
+    }
 }
 
 }  // namespace
@@ -326,16 +332,28 @@ void finish_graph(Ctx &c) {
         k_nlow<<<grid_for(n, TPB), TPB, 0, s>>>(n, g.indices, g.adj, g.nlow);
         CK_LAUNCH("k_nlow");
     }
-    uint32_t lo = 0;   // class 0 includes degree 0 (possible in a transferred graph; convert never keeps one)
-    for (int k = 0; k < DegreeClasses::K; k++) {
-        g.cls.count[k] = class_list(c, lo, DegreeClasses::upper[k], &g.cls.list[k]);
-        lo = DegreeClasses::upper[k] + 1;
+    {   // the degree classes and the long rows; class 0 includes degree 0 (possible in a
+        // transferred graph; convert never keeps one)
+        constexpr int K = DegreeClasses::K;
+        uint32_t lo[K + 1], hi[K + 1], cnt[K + 1];
+        uint32_t *lists[K + 1];
+        for (int k = 0; k < K; k++) {
+            lo[k] = k ? DegreeClasses::upper[k - 1] + 1 : 0u;
+            hi[k] = DegreeClasses::upper[k];
+        }
+        lo[K] = RowWork::CHUNK + 1;
+        hi[K] = 0xffffffffu;
+        class_lists(c, K + 1, lo, hi, lists, cnt);
+        for (int k = 0; k < K; k++) {
+            g.cls.list[k] = lists[k];
+            g.cls.count[k] = cnt[k];
+        }
+        g.rows.llong = lists[K];
+        g.rows.nlong = cnt[K];
     }
     {
         RowWork &rw = g.rows;
-        uint32_t *llong = nullptr;
-        rw.nlong = class_list(c, RowWork::CHUNK + 1, 0xffffffffu, &llong);
-        rw.llong = llong;
+        const uint32_t *llong = rw.llong;
         uint32_t *coff = c.alloc<uint32_t>((size_t)rw.nlong + 1);
         scan_exclusive<uint32_t>(ChunksOf{llong, g.indices}, coff, rw.nlong, s);
         CK(cudaMemcpyAsync(&rw.nchunks, coff + rw.nlong, 4, cudaMemcpyDeviceToHost, s));

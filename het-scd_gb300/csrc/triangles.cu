@@ -572,19 +572,27 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
     plan.dir_lo = split ? b0 : 0;
     plan.dir_hi = split ? B2 : 0;
     plan.dir_amin = c.tc_amin < sm ? c.tc_amin : sm;
+    // every bucket's scans first, then one host read of all the counts
+    DevBuf<uint32_t> pos[TcPlan::K], ipos[TcPlan::K], counts(2 * TcPlan::K, s);
     for (int k = 0; k < TcPlan::K; k++) {
         const bool cta = k == 3 || k == 4;
-        const InBucket fa{o, bounds[k], bounds[k + 1], false}, fb{o, bounds[k], bounds[k + 1], true};
-        DevBuf<uint32_t> pos((size_t)o.n + 1, s), ipos(split && cta ? (size_t)o.n + 1 : 1, s);
-        scan_exclusive<uint32_t>(fa, pos.get(), o.n, s);
-        uint32_t na = 0, nb = 0;
-        CK(cudaMemcpyAsync(&na, pos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+        pos[k].alloc((size_t)o.n + 1, s);
+        scan_exclusive<uint32_t>(InBucket{o, bounds[k], bounds[k + 1], false}, pos[k].get(), o.n, s);
+        CK(cudaMemcpyAsync(counts.get() + 2 * k, pos[k].get() + o.n, 4, cudaMemcpyDeviceToDevice, s));
         if (split && cta) {
-            scan_exclusive<uint32_t>(fb, ipos.get(), o.n, s);
-            CK(cudaMemcpyAsync(&nb, ipos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+            ipos[k].alloc((size_t)o.n + 1, s);
+            scan_exclusive<uint32_t>(InBucket{o, bounds[k], bounds[k + 1], true}, ipos[k].get(), o.n, s);
+            CK(cudaMemcpyAsync(counts.get() + 2 * k + 1, ipos[k].get() + o.n, 4, cudaMemcpyDeviceToDevice, s));
+        } else {
+            CK(cudaMemsetAsync(counts.get() + 2 * k + 1, 0, 4, s));
         }
-        CK(cudaStreamSynchronize(s));
-        const uint32_t cnt = na + nb;
+    }
+    uint32_t cnts[2 * TcPlan::K];
+    CK(cudaMemcpyAsync(cnts, counts.get(), sizeof cnts, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int k = 0; k < TcPlan::K; k++) {
+        const InBucket fa{o, bounds[k], bounds[k + 1], false}, fb{o, bounds[k], bounds[k + 1], true};
+        const uint32_t na = cnts[2 * k], nb = cnts[2 * k + 1], cnt = na + nb;
         plan.nverts[k] = cnt;
         plan.nfwd[k] = na;
         if (owned) {
@@ -597,11 +605,11 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
             plan.unit_off[k] = plan.tmp[2 * k + 1].get();
         }
         if (na) {
-            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, fa, pos.get(), plan.verts[k]);
+            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, fa, pos[k].get(), plan.verts[k]);
             CK_LAUNCH("k_bucket_scatter");
         }
         if (nb) {
-            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, fb, ipos.get(), plan.verts[k] + na);
+            k_bucket_scatter<<<grid_for(o.n, 256), 256, 0, s>>>(o.n, fb, ipos[k].get(), plan.verts[k] + na);
             CK_LAUNCH("k_bucket_scatter");
         }
         scan_exclusive<uint32_t>(UnitsOf{o, plan.verts[k], per_unit[k], na}, plan.unit_off[k], cnt, s);
