@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(W * 32)
 k_sort_rows_cta(const uint32_t *__restrict__ list, uint32_t count, const uint32_t *__restrict__ off, uint32_t *vals,
                 bool dedup, uint32_t *udeg) {
     constexpr int THREADS = W * 32;
-    constexpr uint32_t N = (uint32_t)THREADS * E, WSPAN = 32u * E;
-    extern __shared__ uint32_t sh[];   // N values
+    constexpr uint32_t WSPAN = 32u * E;
+    extern __shared__ uint32_t sh[];   // THREADS * E values
     __shared__ uint32_t wsum[W];
     const uint32_t base = threadIdx.x * E;
     for (uint32_t i = blockIdx.x; i < count; i += gridDim.x) {

@@ -139,13 +139,6 @@ __global__ void k_fill_gid(uint32_t n, uint32_t G, const uint32_t *__restrict__ 
     }
 }
 
-__global__ void k_mark_labels(uint32_t n, const uint32_t *__restrict__ labels, uint32_t *seen, uint32_t nc) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const uint32_t l = labels[v];
-        if (l != INVALID && l < nc) seen[l] = 1;
-    }
-}
-
 __global__ void k_max_label(uint32_t n, const uint32_t *__restrict__ labels, uint32_t *out) {
     uint32_t m = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
@@ -600,20 +593,6 @@ void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int ma
     out.ms_iterations = t2 - t1;
 }
 
-uint32_t distinct_labels(Ctx &c, const uint32_t *labels) {
-    const Graph &g = c.g;
-    cudaStream_t s = c.stream;
-    if (g.n == 0 || c.num_comms == 0) return 0;
-    DevBuf<uint32_t> seen(c.num_comms, s), pre((size_t)c.num_comms + 1, s);
-    CK(cudaMemsetAsync(seen.get(), 0, (size_t)c.num_comms * 4, s));
-    k_mark_labels<<<grid_for(g.n, TPB), TPB, 0, s>>>(g.n, labels, seen.get(), c.num_comms);
-    CK_LAUNCH("k_mark_labels");
-    scan_exclusive<uint32_t>((const uint32_t *)seen.get(), pre.get(), c.num_comms, s);
-    uint32_t cnt = 0;
-    CK(cudaMemcpyAsync(&cnt, pre.get() + c.num_comms, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    return cnt;
-}
 
 
 }  // namespace
