@@ -95,6 +95,17 @@ def lib():
     return _LIB
 
 
+def chosen_in_list_min(report, small_max, warp_max, cta_max):
+    """The in-list split of the autotuner's choice: not an ABI output, it is read from the
+    report line (the fastest among the lines of the chosen three splits)."""
+    head = f"small<={small_max} warp<={warp_max} cta<={cta_max} in-list>"
+    lines = [ln for ln in report if ln.startswith(head)]
+    if not lines:
+        return None
+    best = min(lines, key=lambda ln: float(ln.rsplit(":", 1)[1].split()[0]))
+    return int(best[len(head):].split(":")[0])
+
+
 def header_symbols():
     """Names of the functions include/scd_gb300.h declares."""
     import re
@@ -316,13 +327,9 @@ class Engine:
         self._check(lib().scd_autotune(self._ctx, ctypes.byref(sm), ctypes.byref(w), ctypes.byref(c),
                                        ctypes.byref(ms), buf, 8192))
         report = buf.value.decode().splitlines()
-        # the in-list split is not an ABI output: it is in the report line of the chosen split
-        chosen = f"small<={sm.value} warp<={w.value} cta<={c.value} in-list>"
-        best = min((ln for ln in report if ln.startswith(chosen)), default=None,
-                   key=lambda ln: float(ln.rsplit(":", 1)[1].split()[0]))
-        in_list_min = int(best[len(chosen):].split(":")[0]) if best else None
-        return dict(small_max=sm.value, warp_max=w.value, cta_max=c.value, in_list_min=in_list_min,
-                    best_ms=ms.value, report=report)
+        return dict(small_max=sm.value, warp_max=w.value, cta_max=c.value,
+                    in_list_min=chosen_in_list_min(report, sm.value, w.value, c.value), best_ms=ms.value,
+                    report=report)
 
     def stream(self):
         p = ctypes.c_void_p()

@@ -48,3 +48,12 @@ def test_planted_partition_shape():
     e = scdgen.planted(10000, 18.0, 0.1, 20, 100, seed=1)
     deg = np.bincount(e.ravel(), minlength=10000)
     assert abs(deg.mean() - 20.0) < 1.0   # 18 internal + 2 external on average
+
+
+def test_autotune_report_gives_the_chosen_in_list_split():
+    report = ["small<=32 warp<=64 cta<=512 in-list>0: 3.210 ms",
+              "small<=32 warp<=64 cta<=512 in-list>16: 2.950 ms",
+              "small<=32 warp<=64 cta<=512 in-list>32: 3.001 ms",
+              "small<=16 warp<=64 cta<=512 in-list>16: 1.000 ms"]   # another split, not chosen
+    assert S.chosen_in_list_min(report, 32, 64, 512) == 16
+    assert S.chosen_in_list_min(report, 0, 16, 256) is None
