@@ -222,11 +222,15 @@ int scd_batch_labels_all(scd_ctx *ctx, uint32_t *labels, uint64_t *vertex_offset
 
 /* Autotuner: times the triangle-counting work split on the resident graph over
  * a small grid and keeps the fastest for this context's later conversions and
- * WCC passes.  The split is by out-list length: up to small_max (0, 16 or 32) a
- * group of 16 or 32 lanes intersects in registers; up to warp_max a warp takes
- * 32 list entries at a time against a shared-memory hash table; up to cta_max a
- * 128-thread CTA does, longer lists go to 256-thread CTAs.  report (nullable,
- * report_cap bytes) receives one line per candidate. */
+ * WCC passes (the current split stays unless another is at least 5 % faster).
+ * The split is by out-list length: up to small_max (0, 16 or 32) a group of 16
+ * or 32 lanes intersects in registers; up to warp_max a warp takes 32 list
+ * entries at a time against a shared-memory hash table; up to cta_max a
+ * 128-thread CTA does, longer lists go to 256-thread CTAs.  A fourth dimension,
+ * the out-list length (0, 16 or 32) above which an edge may be counted at its
+ * higher endpoint's table, is reported in the report line of the chosen split
+ * ("in-list>N").  report (nullable, report_cap bytes) receives one line per
+ * candidate. */
 int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t *cta_max, double *best_ms,
                  char *report, uint64_t report_cap);
 
