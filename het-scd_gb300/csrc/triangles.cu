@@ -2,39 +2,40 @@
 // per-edge "lies on a triangle" flags.
 //
 // Every undirected edge has one out-slot in the out-list of its lower-ranked
-// endpoint.  A triangle {a, b, c} with a -> b, a -> c, b -> c is found once,
-// from a: for b in out(a), every c in out(b) ∩ out(a).  That is all the
-// reference's outputs need (src/convert.cpp:290-340): tri[v] = sum of the
-// per-edge counts at v = 2 x (triangles at v), and tri_deg[v] and the filter
-// need only whether an edge's count is > 0.  So the kernel produces
+// endpoint.  A triangle {a, b, c} with a -> b, a -> c, b -> c is found once:
+// c in out(b) ∩ out(a).  That is all the reference's outputs need
+// (src/convert.cpp:290-340): tri[v] = sum of the per-edge counts at v =
+// 2 x (triangles at v), and tri_deg[v] and the filter need only whether an
+// edge's count is > 0.  So the kernels produce
 //   tcount[v]  triangles at v (tri = 2 tcount),
 //   flag[slot] 1 if the edge of that out-slot lies on a triangle,
-// and never a per-edge counter: a's and b's counts and the (a,b), (a,c) flags
-// are aggregated in shared memory per work unit; the only per-triangle global
-// write is the byte store flag(b,c) = 1 (idempotent, no atomic).
-// The reference's id-oriented merge is quadratic in hub degree; this does
-// sum over a->b of d+(b) hash probes.
-//
-// With labels, only internal triangles count (all three vertices carry the
-// same valid label): compute_wcc's int_tri = 2 tcount and int_tri_deg = number
-// of flagged edges (src/wcc.cpp:84-127).  Only b and the table entries c with
-// a's label take part, so every hit is an internal triangle.
+// and never a per-edge counter: the centre's, the partners' and the table
+// entries' counts and flags are aggregated in shared memory per work unit; the
+// only per-triangle global write is the byte store of the walked slot's flag
+// (idempotent, no atomic).  The reference's id-oriented merge is quadratic in
+// hub degree; this does sum over a->b of min(d+(a), d+(b)) hash probes.
 //
 // Which vertex's table counts a triangle: an edge a -> b whose b has the longer
 // out-list (d+(a) < d+(b), b in the CTA buckets) is b-centric: instead of
 // walking out(b) against a's table, the unit of b walks out(a) against b's
 // table (b's in-lists give the a).  Every triangle a -> b -> c is still found
-// exactly once, at a's table or at b's, and the walk is min(d+(a), d+(b))
-// items instead of d+(b) (on R-MAT graphs less than half).
+// exactly once, at a's table or at b's.
 //
-// Work unit = (vertex a, up to 32 consecutive b of out(a)) for one warp, or
-// (centre, up to 512 partners) for one CTA when the centre's out-list is long.  out(a) is staged in a
-// shared-memory open-addressing table (load <= 1/4 for short lists); the
-// unit's items (b, c in out(b)) are flattened with a prefix sum; a warp takes
-// 256 consecutive items, lane L every 32nd from L (coalesced loads), walking
-// the b boundaries forward; a one-hash bitmap (>= 16 bits per entry) in front
-// of the table answers most lookups, which are misses, with one shared load.  Units are grouped by the out-degree of a into
-// buckets so each kernel's shared memory matches its lists.
+// With labels, only internal triangles count (all three vertices carry the
+// same valid label): only partners and table entries with the centre's label
+// take part.  (compute_wcc gives the kernels internal out-lists instead, which
+// is faster; the label filter stays for callers with whole out-lists.)
+//
+// Work unit = (vertex a, its out-list whole) for a register group, (a, up to
+// 32 consecutive b of out(a)) for one warp, or (centre, up to 512 partners) for
+// one CTA when the centre's out-list is long.  The centre's out-list is staged
+// in a shared-memory open-addressing table with a one-hash bitmap (>= 16 bits
+// per entry) in front, which answers most lookups (misses) with one shared load;
+// the unit's items (partner, c in the partner's walk) are flattened with a
+// prefix sum; a warp takes 256 consecutive items, lane L every 32nd from L
+// (coalesced loads), walking the partner boundaries forward.  Centres are
+// grouped by out-degree into buckets so that each kernel's shared memory
+// matches its lists.
 #include "engine.cuh"
 
 namespace scd {
