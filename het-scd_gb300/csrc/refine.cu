@@ -2,8 +2,9 @@
 // (compute_wcc, src/wcc.cpp:31-141) and the clustering coefficient p_ext
 // (src/graph.cpp:57-68); the label improvement itself is in improve.cu.
 //
-// wcc: internal triangles per edge by the oriented counting kernel restricted
-// to same-label triangles, per-vertex sums, per-vertex WCC terms and a
+// wcc: the internal out-lists (out-neighbours with the vertex's own label), the
+// oriented triangle count on them (internal triangles per vertex and the flags
+// of internal edges on one), per-vertex sums, per-vertex WCC terms and a
 // fixed-order (deterministic) tree reduction.
 #include "engine.cuh"
 #include "rows.cuh"
