@@ -1,11 +1,10 @@
 """Build recipe of the SCD engine and its tools (no cmake; parallel nvcc/g++).
 
-Outputs (all under het-scd_gb300/_build/ and oracle/_build/, git-ignored):
+Outputs (all under het-scd_gb300/_build/, git-ignored):
   libscd_gb300.so   CUDA kernels + the C ABI of include/scd_gb300.h (sm_103a only)
   convert, main-gpu, main   the reference's command lines on top of the C ABI
   libscdgen.so      seeded synthetic graph generators
-  oracle/_build/liboracle.so   the CPU oracle (test infrastructure)
-  oracle/_ref/*     the reference's own CPU binaries, only where its sources exist
+The CPU oracle (test infrastructure) has its own recipe, oracle/build_oracle.py.
 """
 import concurrent.futures as cf
 import os
@@ -15,8 +14,6 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "_build")
-ORACLE = os.path.join(ROOT, "oracle")
-REF_SRC = "/root/reference/src"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["engine.cu", "preprocess.cu", "csr.cu", "text.cu", "triangles.cu", "partition.cu", "refine.cu",
@@ -51,7 +48,6 @@ def nvcc_flags(extra=()):
 
 def build(verbose=False, jobs=None):
     os.makedirs(OUT, exist_ok=True)
-    os.makedirs(os.path.join(ORACLE, "_build"), exist_ok=True)
     jobs = jobs or max(4, os.cpu_count() or 4)
     hdrs = _deps_cuda()
     objs = []
@@ -69,13 +65,6 @@ def build(verbose=False, jobs=None):
         if not _newer(gen_so, [gen_src]):
             tasks.append(ex.submit(_run, ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
                                           "-Wall", gen_src, "-o", gen_so]))
-        orc_so = os.path.join(ORACLE, "_build", "liboracle.so")
-        orc_src = [os.path.join(ORACLE, "scd_oracle.cpp"), os.path.join(ORACLE, "scd_oracle.h")]
-        if not _newer(orc_so, orc_src):
-            tasks.append(ex.submit(_run, ["g++", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-                                          "-Wall", orc_src[0], "-o", orc_so]))
-        if os.path.isdir(REF_SRC):
-            tasks.append(ex.submit(_run, ["sh", os.path.join(ORACLE, "build_ref.sh"), REF_SRC]))
         logs = [t.result() for t in tasks]
     lib = os.path.join(OUT, "libscd_gb300.so")
     if not _newer(lib, objs):

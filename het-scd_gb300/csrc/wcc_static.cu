@@ -120,7 +120,10 @@ k_wcc_static_final(const double *__restrict__ partials, uint32_t parts, uint32_t
     }
 }
 
-// device address of g_wcc_partials, looked up once per device
+// device address of g_wcc_partials per device: set up by the first call on a
+// device, refreshed by every call made outside a stream capture (a device reset
+// or a new primary context reloads the module and moves the array), reused as is
+// by calls made while the stream is being captured
 constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_lock;
 double *g_partials_addr[MAX_DEVICES] = {};
@@ -135,24 +138,32 @@ extern "C" int scd_wcc_static(const uint32_t *indices, const uint32_t *adj, cons
                               double alpha, double *wcc, void *stream) {
     if (n > SCD_WCC_STATIC_MAX_VERTICES) return SCD_ERR_LIMIT;
     if (!indices || !wcc || (n && (!adj || !tri || !tri_deg || !labels || !sizes))) return SCD_ERR_ARG;
+    // an error already pending on this thread belongs to the caller: report it
+    // without clearing it, and without launching anything
+    if (cudaPeekAtLastError() != cudaSuccess) return SCD_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return SCD_ERR_CUDA;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return SCD_ERR_CUDA;
     double *partials = nullptr;
     {
-        // first call on this device: resolve the array's device address (this
-        // first call should come before any stream capture)
         std::lock_guard<std::mutex> hold(g_setup_lock);
-        if (!g_partials_addr[dev]) {
+        if (cap == cudaStreamCaptureStatusNone || !g_partials_addr[dev]) {
+            // a host-side lookup of the array's device address; the first call on
+            // a device must not be made while its stream is being captured
+            if (cap != cudaStreamCaptureStatusNone) return SCD_ERR_STATE;
             void *p = nullptr;
             if (cudaGetSymbolAddress(&p, g_wcc_partials) != cudaSuccess || !p) return SCD_ERR_CUDA;
             g_partials_addr[dev] = (double *)p;
         }
         partials = g_partials_addr[dev];
     }
-    cudaStream_t s = (cudaStream_t)stream;
     const uint32_t parts = n ? (n + CHUNK - 1) / CHUNK : 0;
-    if (parts)
+    if (parts) {
         k_wcc_static_partial<<<parts, TPB, 0, s>>>(n, indices, adj, tri, tri_deg, labels, sizes, alpha, partials);
+        if (cudaGetLastError() != cudaSuccess) return SCD_ERR_CUDA;
+    }
     k_wcc_static_final<<<1, TPB, 0, s>>>(partials, parts, n, wcc);
     return cudaGetLastError() == cudaSuccess ? SCD_OK : SCD_ERR_CUDA;
 }

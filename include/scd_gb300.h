@@ -252,8 +252,17 @@ int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t
  * returns SCD_ERR_LIMIT.  All calls share that array: calls that may overlap
  * on the GPU (different streams without ordering) race and must be ordered by
  * the caller.  The first call on a device looks up the array's device address
- * and should come before any stream capture.
- * Returns SCD_OK, SCD_ERR_ARG (NULL pointer), SCD_ERR_LIMIT or SCD_ERR_CUDA. */
+ * and must come before any stream capture (a first call made while its stream
+ * is being captured returns SCD_ERR_STATE).  Every later call made outside a
+ * capture looks the address up again, so a device reset or a new primary
+ * context (which reloads the library's device code and moves the array) is
+ * picked up; a call made during a capture reuses the address of the last call
+ * outside one, so a device reset between that call and the capture leaves it
+ * stale: make one uncaptured call after a reset before capturing again.
+ * An error already pending on the calling thread (cudaPeekAtLastError) is left
+ * in place and reported as SCD_ERR_CUDA before anything is launched.
+ * Returns SCD_OK, SCD_ERR_ARG (NULL pointer), SCD_ERR_LIMIT, SCD_ERR_STATE or
+ * SCD_ERR_CUDA. */
 #define SCD_WCC_STATIC_MAX_VERTICES (1u << 24)
 int scd_wcc_static(const uint32_t *indices, const uint32_t *adj, const int32_t *tri,
                    const int32_t *tri_deg, const uint32_t *labels, const int32_t *sizes, uint32_t n,

@@ -206,6 +206,36 @@ def run(g, max_iters=200, alpha=1.0, threshold=0.01, keep_trace=True):
                 best_wcc=bw.value, printed_comms=pc.value, times=t.as_dict())
 
 
+def run_from_labels(g, labels, max_iters=200, alpha=1.0, threshold=0.01):
+    """The refinement loop of src/main.cpp:60-82 started from a given labelling
+    (num_communities = largest label + 1, statistics by collect_stats), built
+    from the oracle's collect_stats / improve / wcc restatements."""
+    lab = np.ascontiguousarray(labels, np.uint32).copy()
+    valid = lab[lab != 0xFFFFFFFF]
+    nc = int(valid.max()) + 1 if valid.size else 0
+    p_ext = clustering_coef(g)
+    st = collect_stats(g, lab, nc)
+    w0 = wcc(g, lab, st[0], alpha)
+    best_wcc, best = w0, lab.copy()
+    labs, wccs = [], []
+    it = 0
+    while it < max_iters:
+        it += 1
+        lab = improve(g, p_ext, lab, *st, alpha=alpha)
+        st = collect_stats(g, lab, nc)
+        w = wcc(g, lab, st[0], alpha)
+        if w > best_wcc:
+            best = lab.copy()
+        labs.append(lab.copy())
+        wccs.append(w)
+        if w < best_wcc * (1 + threshold):
+            break
+        best_wcc = w
+    printed, _ = compress_labels(best)
+    return dict(iters=it, initial_labels=np.ascontiguousarray(labels, np.uint32), initial_wcc=w0, num_comms=nc,
+                labels=labs, wcc=wccs, best_labels=best, best_wcc=best_wcc, printed_comms=printed)
+
+
 def threads():
     return lib().orc_threads()
 

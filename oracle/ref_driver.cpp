@@ -7,7 +7,12 @@
  * printed community count.  Test infrastructure: it pins the oracle
  * restatement and produces the golden traces; it is never part of the product.
  *
- * usage: ref_driver <graph file> <trace out> [max iterations]
+ * usage: ref_driver <graph file> <trace out> [max iterations] [labels file]
+ * With a labels file (u32[n], SCD_INVALID_LABEL for none) the loop starts from
+ * that labelling instead of create_initial_partition: the Partition gets those
+ * labels, num_communities = largest label + 1, and the reference's own
+ * collect_stats fills its statistics (what cuda_labels_to_device and the
+ * engine's scd_labels_to_device do).
  * Trace layout (little-endian): "SCDTRACE", u32 n, m, num_comms, iters,
  * f64 p_ext, initial_wcc, best_wcc, u32 printed_comms, u32 labels0[n],
  * i32 sizes0/ext0/int0[num_comms], then per iteration f64 wcc, u32 labels[n],
@@ -40,7 +45,28 @@ int main(int argc, char **argv) {
     if (!g) return 1;
     const unsigned n = g->n;
 
-    Partition *p = create_initial_partition(g);
+    Partition *p = nullptr;
+    if (argc > 4) {
+        FILE *lf = fopen(argv[4], "rb");
+        if (!lf) return 1;
+        p = new Partition;
+        p->labels = new unsigned int[n];
+        if (fread(p->labels, 4, n, lf) != n) {
+            fprintf(stderr, "short labels file\n");
+            return 1;
+        }
+        fclose(lf);
+        unsigned nc = 0;
+        for (unsigned v = 0; v < n; v++)
+            if (p->labels[v] != INVALID_LABEL && p->labels[v] + 1 > nc) nc = p->labels[v] + 1;
+        p->num_communities = nc;
+        p->sizes = new int[n];
+        p->ext_edges = new int[n];
+        p->int_edges = new int[n];
+        collect_stats(g, p);
+    } else {
+        p = create_initial_partition(g);
+    }
     double best_wcc = compute_wcc(g, p, alpha);
     const unsigned nc = p->num_communities;
 

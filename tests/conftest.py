@@ -10,3 +10,10 @@ for sub in ("het-scd_gb300", "oracle", "tests"):
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs through the C ABI of libscd_gb300.so)")
+
+
+def pytest_terminal_summary(terminalreporter):
+    import parity_log
+    line = parity_log.summary()
+    if line:
+        terminalreporter.write_line(line)

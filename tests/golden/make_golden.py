@@ -6,9 +6,21 @@ own `convert` (built unmodified from its sources by oracle/build_ref.sh), and
 the trace of the reference's refinement loop (oracle/ref_driver.cpp linked
 against the reference's graph.cpp/scd.cpp/wcc.cpp, OMP_NUM_THREADS=1).
 
+A case may start from a given labelling instead of the initial partition
+(oracle/ref_driver.cpp's labels argument): wrap_windmill does, to put the int32
+products of the gain model (src/scd.cpp:185-213) past 2^31.
+
+The full-size workloads (R-MAT scale 22, a Chung-Lu graph with hubs of degree
+> 46,341) are too large to commit; for them `--pins` records compact pins in
+pins.json instead: sha256 of the input records, of the reference's graph file
+and of every labelling of its trace, and the exact FP64 values.
+
 Run in the development container, where the reference sources exist:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # fixtures + manifest.json
+    python tests/golden/make_golden.py --pins     # pins.json (reference runs of many minutes)
 """
+import hashlib
+import time
 import gzip
 import json
 import os
@@ -37,15 +49,60 @@ TEXT_CASES = {
 }
 
 
+def windmill_text(blades):
+    """A hub joined to `blades` disjoint triangles (hub, a, b): every edge lies on a
+    triangle, the hub's degree is 2 * blades."""
+    out = []
+    for i in range(blades):
+        a, b = 2 * i + 1, 2 * i + 2
+        out.append(f"0 {a}\n0 {b}\n{a} {b}\n")
+    return "".join(out)
+
+
+WINDMILL_BLADES = 30000                          # hub degree 60,000
+WINDMILL_SPLIT = (25000, 29000)                  # blades in community 0 / 1 / unlabelled
+
+
+def windmill_labels(graph):
+    """The hub (final id 0) and the leaves of the first 25,000 blades in
+    community 0 (size 50,001: the hub's d_in = 50,000, so d_in*(d_in-1) and
+    (r-1)*(r-2) wrap), the next 4,000 blades in community 1 (the hub's d_out for
+    it is 52,000: d_out*(d_out-1) wraps), the last 1,000 blades unlabelled."""
+    import oracle as O
+    g = O.Graph.from_bytes(graph)
+    ind, adj = g.indices, g.adj
+    assert ind[1] - ind[0] == 2 * WINDMILL_BLADES
+    lab = np.full(g.n, 0xFFFFFFFF, np.uint32)
+    lab[0] = 0
+    k = 0
+    done = set()
+    for v in range(1, g.n):
+        if lab[v] != 0xFFFFFFFF or v in done:
+            continue
+        row = adj[ind[v]:ind[v + 1]]
+        w = int(row[row != 0][0])
+        c = 0 if k < WINDMILL_SPLIT[0] else 1 if k < WINDMILL_SPLIT[1] else None
+        if c is not None:
+            lab[v] = lab[w] = c
+        done.update((v, w))
+        k += 1
+    return lab
+
+
 def generated_cases():
     import scdgen
     return {
-        "planted_10k": scdgen.planted(10000, 18.0, 0.1, 20, 100, seed=1),    # the plain-SCD config
-        "planted_2k_mu03": scdgen.planted(2000, 12.0, 0.3, 20, 100, seed=8),
-        "planted_5k_mu04": scdgen.planted(5000, 20.0, 0.4, 20, 100, seed=9),
-        "rmat_12": scdgen.rmat(12, 16, 0.57, 0.19, 0.19, seed=5),
-        "chunglu_20k": scdgen.chunglu(20000, 2.1, 5.0, 2000.0, 0.2, 10, 500, seed=7),
+        "planted_10k": lambda: scdgen.planted(10000, 18.0, 0.1, 20, 100, seed=1),    # the plain-SCD config
+        "planted_2k_mu03": lambda: scdgen.planted(2000, 12.0, 0.3, 20, 100, seed=8),
+        "planted_5k_mu04": lambda: scdgen.planted(5000, 20.0, 0.4, 20, 100, seed=9),
+        "rmat_12": lambda: scdgen.rmat(12, 16, 0.57, 0.19, 0.19, seed=5),
+        "chunglu_20k": lambda: scdgen.chunglu(20000, 2.1, 5.0, 2000.0, 0.2, 10, 500, seed=7),
     }
+
+
+def gz_write(path):
+    """gzip writer with a fixed header time, so regenerated fixtures are byte-stable."""
+    return gzip.GzipFile(path, "wb", compresslevel=9, mtime=0)
 
 
 def text_to_pairs(text):
@@ -59,7 +116,8 @@ def text_to_pairs(text):
         os.unlink(p)
 
 
-def run_case(name, text_path, pairs, manifest, trace=True):
+def run_case(name, text_path, pairs, manifest, trace=True, start_labels=None):
+    """start_labels (graph bytes -> labels): the trace starts from that labelling."""
     import oracle as O
     gpath = os.path.join(HERE, name + ".graph")
     r = subprocess.run([os.path.join(REF, "convert"), text_path, gpath], capture_output=True, text=True)
@@ -67,9 +125,9 @@ def run_case(name, text_path, pairs, manifest, trace=True):
         raise RuntimeError(r.stderr)
     graph = open(gpath, "rb").read()
     os.unlink(gpath)
-    with gzip.open(gpath + ".gz", "wb", compresslevel=9) as f:
+    with gz_write(gpath + ".gz") as f:
         f.write(graph)
-    with gzip.open(os.path.join(HERE, name + ".pairs.npy.gz"), "wb", compresslevel=9) as f:
+    with gz_write(os.path.join(HERE, name + ".pairs.npy.gz")) as f:
         np.save(f, pairs.astype(np.uint32))
     entry = {"edges_in": int(pairs.shape[0]), "graph_bytes": len(graph)}
     g = O.Graph.from_bytes(graph)
@@ -80,14 +138,24 @@ def run_case(name, text_path, pairs, manifest, trace=True):
             f.write(graph)
             tmpg = f.name
         env = dict(os.environ, OMP_NUM_THREADS="1")
-        r = subprocess.run([os.path.join(REF, "ref_driver"), tmpg, tpath, "1000"], capture_output=True,
-                           text=True, env=env)
+        cmd = [os.path.join(REF, "ref_driver"), tmpg, tpath, "1000"]
+        if start_labels is not None:
+            lab = start_labels(graph)
+            lpath = tmpg + ".labels"
+            lab.astype("<u4").tofile(lpath)
+            cmd.append(lpath)
+            with gz_write(os.path.join(HERE, name + ".labels.npy.gz")) as f:
+                np.save(f, lab)
+            entry["start_labels"] = True
+        r = subprocess.run(cmd, capture_output=True, text=True, env=env)
         os.unlink(tmpg)
+        if start_labels is not None:
+            os.unlink(lpath)
         if r.returncode != 0:
             raise RuntimeError(r.stderr)
         raw = open(tpath, "rb").read()
         os.unlink(tpath)
-        with gzip.open(tpath + ".gz", "wb", compresslevel=9) as f:
+        with gz_write(tpath + ".gz") as f:
             f.write(raw)
         tr = O.read_trace(tpath + ".gz")
         entry.update(iters=tr["iters"], num_comms=tr["num_comms"], p_ext=tr["p_ext"].hex(),
@@ -96,21 +164,111 @@ def run_case(name, text_path, pairs, manifest, trace=True):
     manifest[name] = entry
 
 
+# Full-size workloads pinned by hashes (pins.json): the R-MAT graph of the headline
+# benchmark (scale 22), the skewed-degree Chung-Lu stress graph (8M vertices,
+# hubs to ~82k), and a 2M-vertex Chung-Lu graph whose hubs also pass degree
+# 46,341, where the int32 products of the gain model wrap.
+PIN_WORKLOADS = {
+    "rmat_22": ("rmat", dict(scale=22, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=22)),
+    "chunglu_8m": ("chunglu", dict(n=8_000_000, gamma=2.1, wmin=5.0, wmax=200000.0, mu=0.2, smin=10, smax=500,
+                                   seed=3)),
+    "chunglu_2m_hubs": ("chunglu", dict(n=2_000_000, gamma=2.1, wmin=5.0, wmax=200000.0, mu=0.2, smin=10,
+                                        smax=500, seed=3)),
+}
+
+
+def sha256(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def make_pins(names):
+    """Runs the reference's convert (all host threads; its output is integer and
+    thread-count independent) and ref_driver (one thread: the canonical sums) on
+    each workload and records hashes of everything they produce."""
+    import oracle as O
+    import scdgen
+    path = os.path.join(HERE, "pins.json")
+    pins = json.load(open(path)) if os.path.exists(path) else {}
+    tmpdir = tempfile.mkdtemp()
+    for name in names:
+        gen, args = PIN_WORKLOADS[name]
+        pairs = getattr(scdgen, gen)(**args)
+        txt = os.path.join(tmpdir, name + ".txt")
+        scdgen.write_text(txt, pairs)
+        gpath = os.path.join(tmpdir, name + ".graph")
+        t0 = time.time()
+        r = subprocess.run([os.path.join(REF, "convert"), txt, gpath], capture_output=True, text=True,
+                           env=dict(os.environ, OMP_NUM_THREADS=str(os.cpu_count())))
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr)
+        convert_s = time.time() - t0
+        os.unlink(txt)
+        graph = open(gpath, "rb").read()
+        g = O.Graph.from_bytes(graph)
+        deg = np.diff(g.indices.astype(np.int64))
+        tpath = os.path.join(tmpdir, name + ".trace")
+        t0 = time.time()
+        r2 = subprocess.run([os.path.join(REF, "ref_driver"), gpath, tpath, "1000"], capture_output=True, text=True,
+                            env=dict(os.environ, OMP_NUM_THREADS="1"))
+        if r2.returncode != 0:
+            raise RuntimeError(r2.stderr)
+        driver_s = time.time() - t0
+        tr = O.read_trace(tpath)
+        os.unlink(gpath)
+        os.unlink(tpath)
+        pins[name] = {
+            "generator": gen, "args": args, "edges_in": int(pairs.shape[0]), "pairs_sha256": sha256(pairs),
+            "n": g.n, "m": g.m, "max_degree": int(deg.max()) if g.n else 0, "graph_bytes": len(graph),
+            "graph_sha256": hashlib.sha256(graph).hexdigest(),
+            "p_ext": tr["p_ext"].hex(), "num_comms": tr["num_comms"],
+            "initial_labels_sha256": sha256(tr["initial_labels"]),
+            "initial_stats_sha256": sha256(tr["initial_stats"]), "initial_wcc": tr["initial_wcc"].hex(),
+            "iters": tr["iters"], "wcc": [w.hex() for w in tr["wcc"]],
+            "labels_sha256": [sha256(l) for l in tr["labels"]],
+            "stats_sha256": [sha256(st) for st in tr["stats"]],
+            "best_labels_sha256": sha256(tr["best_labels"]), "best_wcc": tr["best_wcc"].hex(),
+            "printed_comms": tr["printed_comms"],
+            "reference_seconds": {"convert": round(convert_s, 1), "convert_threads": os.cpu_count(),
+                                  "ref_driver_1_thread": round(driver_s, 1)},
+            "reference_convert_stdout": [l for l in r.stdout.splitlines() if "lines read" not in l],
+        }
+        with open(path, "w") as f:
+            json.dump(pins, f, indent=1, sort_keys=True)
+        print(name, json.dumps({k: pins[name][k] for k in ("n", "m", "max_degree", "iters", "reference_seconds")}))
+
+
 def main():
+    if "--pins" in sys.argv:
+        names = [a for a in sys.argv[1:] if not a.startswith("--")] or list(PIN_WORKLOADS)
+        if not os.path.exists(os.path.join(REF, "ref_driver")):
+            subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+        return make_pins(names)
     if not os.path.exists(os.path.join(REF, "ref_driver")):
         subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
     import scdgen
-    manifest = {}
+    only = [a for a in sys.argv[1:] if not a.startswith("--")]   # regenerate just these cases
+    mpath = os.path.join(HERE, "manifest.json")
+    manifest = json.load(open(mpath)) if only else {}
     tmpdir = tempfile.mkdtemp()
     for name, text in TEXT_CASES.items():
+        if only and name not in only:
+            continue
         p = os.path.join(tmpdir, name + ".txt")
         open(p, "w").write(text)
         run_case(name, p, text_to_pairs(text), manifest)
-    for name, pairs in generated_cases().items():
+    for name, make in generated_cases().items():
+        if only and name not in only:
+            continue
+        pairs = make()
         p = os.path.join(tmpdir, name + ".txt")
         scdgen.write_text(p, pairs)
         run_case(name, p, pairs, manifest)
-    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+    if not only or "wrap_windmill" in only:
+        text = windmill_text(WINDMILL_BLADES)
+        p = os.path.join(tmpdir, "wrap_windmill.txt")
+        open(p, "w").write(text)
+        run_case("wrap_windmill", p, text_to_pairs(text), manifest, start_labels=windmill_labels)
+    with open(mpath, "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
     print(json.dumps({k: {kk: v[kk] for kk in ("n", "m", "edges_in") if kk in v} | {"iters": v.get("iters")}
                       for k, v in manifest.items()}, indent=1))

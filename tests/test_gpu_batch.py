@@ -23,7 +23,7 @@ def engine():
 
 
 def test_golden_fixtures_as_one_batch(engine):
-    names = G.cases()
+    names = G.partition_cases()
     engine.batch_convert([G.pairs(n) for n in names])
     assert engine.batch_size() == len(names)
     for g, name in enumerate(names):

@@ -14,11 +14,13 @@ import golden_data as G
 import oracle as O
 import scd_gb300 as S
 import scdgen
+from parity_log import log
 
 pytestmark = pytest.mark.gpu
 WCC_RTOL = 1e-6
 CASES = G.cases()
-TRACED = [c for c in CASES if G.manifest()[c].get("iters")]
+TRACED = [c for c in G.partition_cases() if G.manifest()[c].get("iters")]
+FROM_LABELS = [c for c in CASES if G.starts_from_labels(c)]
 
 
 @pytest.fixture(scope="module")
@@ -60,6 +62,8 @@ def test_iterations_match_reference_trace(engine, name):
     for i in range(tr["iters"]):
         w = engine.improve_labels()
         got = engine.current_labels()
+        log(name, f"iteration {i + 1}", labels_equal=bool(np.array_equal(got, tr["labels"][i])), wcc=w.hex(),
+            wcc_ref=tr["wcc"][i].hex(), wcc_rel=rel(w, tr["wcc"][i]))
         assert np.array_equal(got, tr["labels"][i]), f"iteration {i}: " + _divergence_report(
             g, cc, None, None, got, tr["labels"][i])
         assert np.array_equal(np.stack(engine.community_stats()), tr["stats"][i])
@@ -79,6 +83,43 @@ def test_run_loop_matches_reference(engine, name):
     assert r["printed_communities"] == tr["printed_comms"]
     for a, b in zip(r["wcc"], tr["wcc"]):
         assert rel(a, b) < WCC_RTOL
+
+
+@pytest.mark.parametrize("name", FROM_LABELS)
+def test_iterations_from_given_labels_match_reference(engine, name):
+    """wrap_windmill: a hub of degree 60,000 whose community has 50,001 members, so
+    the int32 products d_in*(d_in-1), d_out*(d_out-1) and (r-1)*(r-2) of the gain
+    model (src/scd.cpp:185-213) wrap; labels, statistics and WCC of every
+    iteration against the reference's loop started from the same labels."""
+    g = O.Graph.from_bytes(G.graph_bytes(name))
+    tr = G.trace(name)
+    engine.transfer_graph(g)
+    assert engine.graph_info()[2] == tr["p_ext"]
+    engine.labels_to_device(G.start_labels(name))
+    assert np.array_equal(np.stack(engine.community_stats()), tr["initial_stats"])
+    assert rel(engine.compute_wcc(), tr["initial_wcc"]) < WCC_RTOL
+    for i in range(tr["iters"]):
+        w = engine.improve_labels()
+        got = engine.current_labels()
+        log(name, f"iteration {i + 1} (from given labels)", labels_equal=bool(np.array_equal(got, tr["labels"][i])),
+            wcc=w.hex(), wcc_ref=tr["wcc"][i].hex(), wcc_rel=rel(w, tr["wcc"][i]))
+        assert np.array_equal(got, tr["labels"][i]), f"iteration {i}: " + _divergence_report(
+            g, None, None, None, got, tr["labels"][i])
+        assert np.array_equal(np.stack(engine.community_stats()), tr["stats"][i])
+        assert rel(w, tr["wcc"][i]) < WCC_RTOL
+
+
+@pytest.mark.parametrize("name", FROM_LABELS)
+def test_run_loop_from_given_labels_matches_reference(engine, name):
+    g = O.Graph.from_bytes(G.graph_bytes(name))
+    tr = G.trace(name)
+    engine.transfer_graph(g)
+    engine.labels_to_device(G.start_labels(name))
+    r = engine.run(0.01, 1000)
+    assert r["iterations"] == tr["iters"]
+    assert rel(r["best_wcc"], tr["best_wcc"]) < WCC_RTOL
+    assert np.array_equal(engine.labels_from_device(), tr["best_labels"])
+    assert r["printed_communities"] == tr["printed_comms"]
 
 
 RANDOM_GRAPHS = [

@@ -13,6 +13,8 @@ import golden_data as G
 import oracle as O
 
 CASES = G.cases()
+TRACED = [c for c in G.partition_cases() if G.manifest()[c].get("iters")]
+FROM_LABELS = [c for c in CASES if G.starts_from_labels(c)]
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -21,7 +23,7 @@ def test_convert_matches_reference_file(name):
     assert g.to_bytes() == G.graph_bytes(name)
 
 
-@pytest.mark.parametrize("name", [c for c in CASES if G.manifest()[c].get("iters")])
+@pytest.mark.parametrize("name", TRACED)
 def test_refinement_trace_matches_reference(name):
     g = O.Graph.from_bytes(G.graph_bytes(name))
     tr = G.trace(name)
@@ -39,7 +41,7 @@ def test_refinement_trace_matches_reference(name):
     assert r["printed_comms"] == tr["printed_comms"]
 
 
-@pytest.mark.parametrize("name", [c for c in CASES if G.manifest()[c].get("iters")])
+@pytest.mark.parametrize("name", TRACED + FROM_LABELS)
 def test_statistics_match_reference(name):
     g = O.Graph.from_bytes(G.graph_bytes(name))
     tr = G.trace(name)
@@ -49,6 +51,40 @@ def test_statistics_match_reference(name):
     for it in range(tr["iters"]):
         s, e, i = O.collect_stats(g, tr["labels"][it], nc)
         assert np.array_equal(np.stack([s, e, i]), tr["stats"][it])
+
+
+@pytest.mark.parametrize("name", FROM_LABELS)
+def test_loop_from_given_labels_matches_reference(name):
+    """The reference's loop started from a given labelling (wrap_windmill: the
+    int32 products of the gain model wrap for the hub and its community)."""
+    g = O.Graph.from_bytes(G.graph_bytes(name))
+    tr = G.trace(name)
+    lab = G.start_labels(name)
+    assert np.array_equal(lab, tr["initial_labels"])
+    r = O.run_from_labels(g, lab, max_iters=1000)
+    assert r["num_comms"] == tr["num_comms"]
+    assert r["initial_wcc"] == tr["initial_wcc"]
+    assert r["iters"] == tr["iters"]
+    for i in range(tr["iters"]):
+        assert np.array_equal(r["labels"][i], tr["labels"][i]), f"iteration {i}"
+        assert r["wcc"][i] == tr["wcc"][i]
+    assert np.array_equal(r["best_labels"], tr["best_labels"])
+    assert r["best_wcc"] == tr["best_wcc"]
+    assert r["printed_comms"] == tr["printed_comms"]
+
+
+def test_windmill_reaches_the_int32_wrap():
+    """The wrap_windmill labelling puts d_in*(d_in-1), d_out*(d_out-1) and
+    (r-1)*(r-2) of src/scd.cpp:185-213 past 2^31 for the hub."""
+    g = O.Graph.from_bytes(G.graph_bytes("wrap_windmill"))
+    lab = G.start_labels("wrap_windmill")
+    deg = int(g.indices[1] - g.indices[0])
+    nb = lab[g.adj[g.indices[0]:g.indices[1]]]
+    d_in0 = int((nb == 0).sum())
+    r0 = int((lab == 0).sum()) - 1                 # own community, the hub taken out
+    d_out1 = deg - int((nb == 1).sum())
+    for x in (d_in0, r0 - 1, d_out1):
+        assert x * (x - 1) > 2**31 - 1
 
 
 def test_known_answer_triangle_pendant():

@@ -43,11 +43,11 @@ def _static_wcc(lib, torch, graph, labels, sizes, alpha=1.0):
     return float(out.item())
 
 
-def test_static_wcc_matches_engine_on_two_calls_in_a_row():
-    torch = pytest.importorskip("torch")
-    lib = S.lib()
+def _engine_pair(name):
+    """The engine's WCC, labels and community sizes of the initial partition and
+    of the first iteration of a golden case."""
     with S.Engine(0) as eng:
-        eng.convert_edges(G.pairs("planted_10k"))
+        eng.convert_edges(G.pairs(name))
         graph = eng.graph_download()
         eng.initial_partition()
         want = [eng.compute_wcc()]
@@ -56,10 +56,47 @@ def test_static_wcc_matches_engine_on_two_calls_in_a_row():
         want.append(eng.improve_labels())
         labels.append(eng.current_labels())
         sizes.append(eng.community_stats()[0].copy())
+    return graph, want, labels, sizes
+
+
+@pytest.mark.parametrize("name", ["planted_10k", "rmat_12", "chunglu_20k"])
+def test_static_wcc_matches_engine_on_two_calls_in_a_row(name):
+    """Same terms and the same summation order as scd_compute_wcc: equal bit for
+    bit, on two calls in a row (the second sees the second labelling).  The
+    R-MAT and Chung-Lu cases have hub rows; planted_10k ends in a partly full
+    block of 2048 vertices."""
+    torch = pytest.importorskip("torch")
+    lib = S.lib()
+    graph, want, labels, sizes = _engine_pair(name)
     got = [_static_wcc(lib, torch, graph, labels[k], sizes[k]) for k in range(2)]
-    for g, w in zip(got, want):
-        assert abs(g - w) <= RTOL * abs(w), (g, w)
-    assert got[0] != got[1]   # the second call saw the second labelling
+    assert got == want, (got, want)
+    assert abs(got[0] - want[0]) <= RTOL * abs(want[0])
+    assert got[0] != got[1]
+
+
+def test_static_wcc_skip_branches_match_engine():
+    """A labelling with unlabelled vertices and communities of one and two
+    vertices (the terms the reference skips: INVALID label, size <= 2)."""
+    torch = pytest.importorskip("torch")
+    lib = S.lib()
+    with S.Engine(0) as eng:
+        eng.convert_edges(G.pairs("planted_10k"))
+        graph = eng.graph_download()
+        eng.initial_partition()
+        lab = eng.current_labels().copy()
+        n = lab.size
+        rng = np.random.default_rng(3)
+        lab[rng.choice(n, n // 10, replace=False)] = S.INVALID_LABEL
+        a, b = np.unique(lab[lab != S.INVALID_LABEL])[:2]   # two labels in use: a keeps 2 vertices, b one
+        lab[(lab == a) | (lab == b)] = S.INVALID_LABEL
+        lab[0] = lab[1] = a
+        lab[2] = b
+        eng.labels_to_device(lab)
+        want = eng.compute_wcc()
+        sizes = eng.community_stats()[0].copy()
+    assert sizes[a] == 2 and sizes[b] == 1 and (lab == S.INVALID_LABEL).any()
+    got = _static_wcc(lib, torch, graph, lab, sizes)
+    assert got == want, (got, want)
 
 
 def test_static_wcc_limits_and_arguments():
