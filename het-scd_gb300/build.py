@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["engine.cu", "preprocess.cu", "csr.cu", "text.cu", "triangles.cu", "partition.cu", "refine.cu",
-              "improve.cu", "wcc_static.cu"]
+              "improve.cu", "resident.cu", "wcc_static.cu"]
 
 
 def _run(cmd, cwd=None):

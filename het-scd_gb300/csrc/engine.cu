@@ -266,31 +266,20 @@ void Ctx::free_all() {
     num_comms = 0;
 }
 
-void finish_graph(Ctx &c) {
+// The derived structure of the (union) graph: nlow, the graph of each vertex,
+// the graph-aligned WCC blocks, degree classes, row work, the global hash tables,
+// the iteration's scratch arrays and the triangle-counting plan.  Needs
+// g.indices/adj, b.G, b.h_fin_off and b.fin_off; always_gid: a graph-id array even
+// for one graph (resident sets run every kernel in the skip-converged-graphs mode).
+void build_union_structure(Ctx &c, bool always_gid) {
     Graph &g = c.g;
+    Batch &b = c.b;
     cudaStream_t s = c.stream;
     const uint32_t n = g.n;
     g.nlow = c.alloc<uint32_t>(n);
     prepare_tc_kernels();
     prepare_improve_kernels();
-    // per-graph bookkeeping of the (possibly one-graph) batch
-    Batch &b = c.b;
-    if (!b.fin_off) {
-        b.fin_off = c.alloc<uint32_t>(b.G + 1);
-        CK(cudaMemcpyAsync(b.fin_off, b.h_fin_off.data(), 4 * (b.G + 1), cudaMemcpyHostToDevice, s));
-    }
-    CK(cudaStreamSynchronize(s));   // h_fin_off is complete
-    {
-        std::vector<uint32_t> ind_at(b.G + 1);
-        DevBuf<uint32_t> tmp(b.G + 1, s);
-        k_gather_indices<<<grid_for(b.G + 1, TPB), TPB, 0, s>>>(b.G, b.fin_off, g.indices, tmp.get());
-        CK_LAUNCH("k_gather_indices");
-        CK(cudaMemcpyAsync(ind_at.data(), tmp.get(), 4 * (b.G + 1), cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        b.h_m.resize(b.G);
-        for (uint32_t k = 0; k < b.G; k++) b.h_m[k] = (ind_at[k + 1] - ind_at[k]) / 2;
-    }
-    if (b.G > 1) {
+    if (b.G > 1 || always_gid) {
         b.gid = c.alloc<uint32_t>(n);
         if (n) {
             k_fill_gid<<<grid_for(n, TPB), TPB, 0, s>>>(n, b.G, b.fin_off, b.gid);
@@ -312,15 +301,6 @@ void finish_graph(Ctx &c) {
         if (b.blocks) CK(cudaMemcpyAsync(b.blk_gid, blk_gid.data(), 4 * b.blocks, cudaMemcpyHostToDevice, s));
         CK(cudaStreamSynchronize(s));
     }
-    b.p_ext = c.alloc<double>(b.G);
-    b.pe32 = c.alloc<float2>(b.G);
-    b.comm_off = c.alloc<uint32_t>(b.G + 1);
-    b.wcc = c.alloc<double>(b.G);
-    b.best_wcc = c.alloc<double>(b.G);
-    b.active = c.alloc<uint8_t>(b.G);
-    b.improved = c.alloc<uint8_t>(b.G);
-    b.iters = c.alloc<int32_t>(b.G);
-    b.n_active = c.alloc<uint32_t>(1);
     if (n) {
         k_nlow<<<grid_for(n, TPB), TPB, 0, s>>>(n, g.indices, g.adj, g.nlow);
         CK_LAUNCH("k_nlow");
@@ -355,19 +335,13 @@ void finish_graph(Ctx &c) {
     }
     const uint32_t n_big = g.cls.count[DegreeClasses::K - 1];
     g.big_table_off = c.alloc<uint64_t>((size_t)n_big + 1);
+    g.big_table_words = 0;
+    c.big_tables = nullptr;
     if (n_big) {
         scan_exclusive<uint64_t>(TableWords{g.cls.list[DegreeClasses::K - 1], g.indices}, g.big_table_off, n_big, s);
         CK(cudaMemcpyAsync(&g.big_table_words, g.big_table_off + n_big, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         c.big_tables = c.alloc<uint32_t>(g.big_table_words);
-    }
-    c.labels = c.alloc<uint32_t>(n);
-    c.labels_next = c.alloc<uint32_t>(n);
-    c.best = c.alloc<uint32_t>(n);
-    for (int k = 0; k < 2; k++) {
-        c.st[k].sizes = c.alloc<int32_t>(n);
-        c.st[k].ext = c.alloc<int32_t>(n);
-        c.st[k].intl = c.alloc<int32_t>(n);
     }
     c.pin64 = c.alloc<double>(n);
     c.civ = c.alloc<int4>(n);
@@ -376,19 +350,90 @@ void finish_graph(Ctx &c) {
     c.itdeg = c.alloc<int32_t>(n);
     c.int_len = c.alloc<uint32_t>(n);
     c.int_adj = c.alloc<uint32_t>(2 * (size_t)g.m);
+    c.wplan = TcPlan();
     if (n) tc_plan(c, Oriented{g.indices, g.nlow, g.adj, n}, c.wplan, s, true, false);
     c.wcc_part = c.alloc<double>(b.blocks + 1);
+    c.launches += 3;
+}
+
+void finish_graph(Ctx &c) {
+    Graph &g = c.g;
+    cudaStream_t s = c.stream;
+    const uint32_t n = g.n;
+    // per-graph bookkeeping of the (possibly one-graph) batch
+    Batch &b = c.b;
+    if (!b.fin_off) {
+        b.fin_off = c.alloc<uint32_t>(b.G + 1);
+        CK(cudaMemcpyAsync(b.fin_off, b.h_fin_off.data(), 4 * (b.G + 1), cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));   // h_fin_off is complete
+    {
+        std::vector<uint32_t> ind_at(b.G + 1);
+        DevBuf<uint32_t> tmp(b.G + 1, s);
+        k_gather_indices<<<grid_for(b.G + 1, TPB), TPB, 0, s>>>(b.G, b.fin_off, g.indices, tmp.get());
+        CK_LAUNCH("k_gather_indices");
+        CK(cudaMemcpyAsync(ind_at.data(), tmp.get(), 4 * (b.G + 1), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        b.h_m.resize(b.G);
+        for (uint32_t k = 0; k < b.G; k++) b.h_m[k] = (ind_at[k + 1] - ind_at[k]) / 2;
+    }
+    b.p_ext = c.alloc<double>(b.G);
+    b.pe32 = c.alloc<float2>(b.G);
+    b.comm_off = c.alloc<uint32_t>(b.G + 1);
+    b.wcc = c.alloc<double>(b.G);
+    b.best_wcc = c.alloc<double>(b.G);
+    b.active = c.alloc<uint8_t>(b.G);
+    b.improved = c.alloc<uint8_t>(b.G);
+    b.iters = c.alloc<int32_t>(b.G);
+    b.n_active = c.alloc<uint32_t>(1);
+    c.labels = c.alloc<uint32_t>(n);
+    c.labels_next = c.alloc<uint32_t>(n);
+    c.best = c.alloc<uint32_t>(n);
+    for (int k = 0; k < 2; k++) {
+        c.st[k].sizes = c.alloc<int32_t>(n);
+        c.st[k].ext = c.alloc<int32_t>(n);
+        c.st[k].intl = c.alloc<int32_t>(n);
+    }
+    build_union_structure(c, false);
     compute_p_ext(c);
-    c.launches += 4;
+    c.launches++;
+}
+
+// One refinement iteration for every graph still running, without host
+// synchronisation (so it can be captured in a CUDA graph): improve, statistics,
+// WCC, per-graph loop control.
+void iterate_async(Ctx &c, double threshold, double *trace, int max_trace) {
+    // converged graphs of a batch or a resident set keep their labels; their statistics
+    // and WCC are not needed any more
+    const bool frozen = c.b.G > 1 || c.resident;
+    improve(c, c.labels, c.st[c.cur], c.labels_next, frozen);
+    uint32_t *t = c.labels;
+    c.labels = c.labels_next;
+    c.labels_next = t;
+    c.cur ^= 1;
+    collect_stats(c, c.labels, c.st[c.cur], frozen);
+    launch_wcc(c, c.labels, c.st[c.cur], frozen);
+    batch_step(c, threshold, trace, max_trace);
+}
+
+// Kernel nodes of a captured graph (the launches one replay makes).
+uint64_t kernel_nodes(cudaGraph_t gr) {
+    size_t n = 0;
+    CK(cudaGraphGetNodes(gr, nullptr, &n));
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n) CK(cudaGraphGetNodes(gr, nodes.data(), &n));
+    uint64_t k = 0;
+    for (size_t i = 0; i < n; i++) {
+        cudaGraphNodeType t;
+        CK(cudaGraphNodeGetType(nodes[i], &t));
+        k += t == cudaGraphNodeTypeKernel;
+    }
+    return k;
 }
 
 }  // namespace scd
 
 using namespace scd;
-
-struct scd_ctx {
-    Ctx c;
-};
 
 namespace {
 
@@ -460,21 +505,6 @@ double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// One refinement iteration for every graph still running, without host
-// synchronisation (so it can be captured in a CUDA graph): improve, statistics,
-// WCC, per-graph loop control.
-void iterate_async(Ctx &c, double threshold, double *trace, int max_trace) {
-    improve(c, c.labels, c.st[c.cur], c.labels_next, c.b.G > 1);
-    uint32_t *t = c.labels;
-    c.labels = c.labels_next;
-    c.labels_next = t;
-    c.cur ^= 1;
-    // converged graphs of a batch keep their labels; their statistics and WCC are not needed any more
-    collect_stats(c, c.labels, c.st[c.cur], c.b.G > 1);
-    launch_wcc(c, c.labels, c.st[c.cur], c.b.G > 1);
-    batch_step(c, threshold, trace, max_trace);
-}
-
 struct RunOut {
     std::vector<double> wcc0, best;
     std::vector<int32_t> iters;
@@ -505,21 +535,6 @@ std::vector<uint32_t> distinct_per_graph(Ctx &c, const uint32_t *labels) {
 // The loop of src/main-gpu.cpp:54-95 for every graph of the context at once;
 // each iteration is replayed from a captured CUDA graph (two graphs, one per
 // parity of the label double buffer), with one host read per iteration.
-// Kernel nodes of a captured graph (the launches one replay makes).
-static uint64_t kernel_nodes(cudaGraph_t gr) {
-    size_t n = 0;
-    CK(cudaGraphGetNodes(gr, nullptr, &n));
-    std::vector<cudaGraphNode_t> nodes(n);
-    if (n) CK(cudaGraphGetNodes(gr, nodes.data(), &n));
-    uint64_t k = 0;
-    for (size_t i = 0; i < n; i++) {
-        cudaGraphNodeType t;
-        CK(cudaGraphNodeGetType(nodes[i], &t));
-        k += t == cudaGraphNodeTypeKernel;
-    }
-    return k;
-}
-
 void run_loop(Ctx &c, double threshold, int max_iters, double *trace_dev, int max_trace, RunOut &out) {
     Batch &b = c.b;
     cudaStream_t s = c.stream;
@@ -635,6 +650,7 @@ void scd_destroy(scd_ctx *ctx) {
     if (!ctx) return;
     Ctx &c = ctx->c;
     cudaSetDevice(c.device);
+    resident_destroy(c);
     c.free_all();
     if (c.stream) cudaStreamSynchronize(c.stream);
     {   // hand the cached pool memory back (arrays still in use elsewhere are not affected)
@@ -1131,6 +1147,10 @@ int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t
             report[report_cap - 1] = 0;
         }
     });
+}
+
+int scd_set_memory_limit(scd_ctx *ctx, uint64_t bytes) {
+    return guarded(ctx, [&](Ctx &c) { c.mem_limit = bytes; });
 }
 
 int scd_memory_usage(scd_ctx *ctx, uint64_t *bytes) {

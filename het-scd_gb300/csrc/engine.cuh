@@ -168,6 +168,8 @@ struct PhaseScope {
     ~PhaseScope();
 };
 
+struct ResidentSet;   // resident.cu: graphs that join and leave between iterations
+
 struct Ctx {
     int device = 0;
     int work_group_size = 256;
@@ -209,6 +211,9 @@ struct Ctx {
     int4 *civ = nullptr;              // size, external edges and the FP32 enclosure of p_in (bits)
     uint32_t *work_counter = nullptr; // dynamic work distribution
 
+    ResidentSet *res = nullptr;       // set by scd_resident_init
+    bool resident = false;            // every iteration skips the graphs that stopped
+
     PhaseTimers timers;
     std::vector<void *> owned;        // device allocations freed with the graph
     uint64_t bytes = 0;
@@ -216,10 +221,14 @@ struct Ctx {
     // graph-lifetime device arrays: stream-ordered from the device's memory pool, which
     // keeps freed memory cached (release threshold raised at scd_create), so a new graph
     // reuses the previous one's memory without cudaMalloc/cudaFree synchronisation
+    uint64_t mem_limit = 0;           // scd_set_memory_limit (0: none)
+
     template <typename T>
     T *alloc(size_t count) {
         void *p = nullptr;
         if (count == 0) count = 1;
+        if (mem_limit && bytes + count * sizeof(T) > mem_limit)
+            throw Error(SCD_ERR_OOM, "device memory limit of the context reached");
         CK(cudaMallocAsync(&p, count * sizeof(T), stream));
         owned.push_back(p);
         bytes += count * sizeof(T);
@@ -239,6 +248,15 @@ void alloc_graph(Ctx &c, uint32_t n, uint32_t m);
 void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const uint32_t *adj,
                   const int32_t *tri, const int32_t *tri_deg);
 void finish_graph(Ctx &c);   // nlow, p_ext, degree classes, partition buffers
+// the derived structure of the union graph (see engine.cu); always_gid: a graph-id
+// array even for one graph
+void build_union_structure(Ctx &c, bool always_gid);
+// engine.cu: one refinement iteration of every running graph without host
+// synchronisation (capturable); kernel nodes of a captured CUDA graph
+void iterate_async(Ctx &c, double threshold, double *trace, int max_trace);
+uint64_t kernel_nodes(cudaGraph_t gr);
+// resident.cu
+void resident_destroy(Ctx &c);
 
 
 // partition.cu
@@ -260,3 +278,8 @@ void batch_step(Ctx &c, double threshold, double *trace = nullptr, int max_trace
 void batch_reset(Ctx &c);   // best := current WCC, all non-empty graphs active
 
 }  // namespace scd
+
+// the opaque handle of the C ABI
+struct scd_ctx {
+    scd::Ctx c;
+};

@@ -86,6 +86,13 @@ def lib():
                               ctypes.c_char_p, u64], i32),
             "scd_load_graph_file": ([P, ctypes.c_char_p, dbl], i32),
             "scd_transfer_graph_bytes": ([P, ctypes.c_char_p, u64, dbl], i32),
+            "scd_set_memory_limit": ([P, u64], i32),
+            "scd_resident_init": ([P, dbl, i32], i32),
+            "scd_resident_add": ([P, P, P], i32),
+            "scd_resident_step": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32)], i32),
+            "scd_resident_take": ([P, u32, P, P, P, P, u64, P, ctypes.POINTER(u32)], i32),
+            "scd_resident_info": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32),
+                                   ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(u64)], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -261,6 +268,9 @@ class Engine:
         d["wcc"] = trace[: r.iterations].copy()
         return d
 
+    def set_memory_limit(self, nbytes):
+        self._check(lib().scd_set_memory_limit(self._ctx, int(nbytes)))
+
     def memory_usage(self):
         b = ctypes.c_uint64()
         self._check(lib().scd_memory_usage(self._ctx, ctypes.byref(b)))
@@ -343,6 +353,49 @@ class Engine:
 
     def profile_reset(self):
         self._check(lib().scd_profile_reset(self._ctx))
+
+    # --- resident set (continuous batching) ---------------------------------
+    def resident_init(self, threshold=0.01, max_iters=1000):
+        """Makes this engine an empty resident set (scd_resident_init)."""
+        self._check(lib().scd_resident_init(self._ctx, threshold, max_iters))
+
+    def resident_add(self, src):
+        """Moves every graph resident in engine `src` into this set; returns their ids."""
+        G = src.batch_size() if src.has_graph() else 0
+        ids = np.zeros(max(G, 1), np.uint64)
+        self._check(lib().scd_resident_add(self._ctx, src._ctx, _p(ids)))
+        return [int(i) for i in ids[:G]]
+
+    def resident_step(self):
+        """One iteration of every running graph (graphs waiting to join are merged
+        in first); returns (graphs that iterated, graphs that stopped in this step)."""
+        run, fin = ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(lib().scd_resident_step(self._ctx, ctypes.byref(run), ctypes.byref(fin)))
+        return run.value, fin.value
+
+    def resident_take(self, cap=1 << 16, labels_cap=1 << 26):
+        """Stopped graphs with their results: a list of (id, result dict, status, labels)."""
+        ids = np.zeros(cap, np.uint64)
+        res = (Result * cap)()
+        status = np.zeros(cap, np.int32)
+        labels = np.empty(max(labels_cap, 1), np.uint32)
+        off = np.zeros(cap + 1, np.uint64)
+        cnt = ctypes.c_uint32()
+        self._check(lib().scd_resident_take(self._ctx, cap, _p(ids), res, _p(status), _p(labels), labels_cap,
+                                            _p(off), ctypes.byref(cnt)))
+        return [(int(ids[k]), res[k].as_dict(), int(status[k]), labels[int(off[k]):int(off[k + 1])].copy())
+                for k in range(cnt.value)]
+
+    def resident_info(self):
+        g, r, p = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        st, gs, kp = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(lib().scd_resident_info(self._ctx, ctypes.byref(g), ctypes.byref(r), ctypes.byref(p),
+                                            ctypes.byref(st), ctypes.byref(gs), ctypes.byref(kp)))
+        return dict(graphs=g.value, running=r.value, pending=p.value, steps=st.value, graph_steps=gs.value,
+                    kernels_per_step=kp.value)
+
+    def has_graph(self):
+        return lib().scd_batch_size(self._ctx, ctypes.byref(ctypes.c_uint32())) == OK
 
     def kernel_launches(self):
         b = ctypes.c_uint64()

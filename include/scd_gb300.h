@@ -167,6 +167,13 @@ int scd_run(scd_ctx *ctx, double threshold, int max_iters, double *wcc_trace, sc
 
 /* Device memory currently held by the context (bytes). */
 int scd_memory_usage(scd_ctx *ctx, uint64_t *bytes);
+/* A cap on the device memory the context holds for its graphs (0: none): an
+ * allocation that would pass it fails with SCD_ERR_OOM, as a failed cudaMalloc
+ * does, and the context stays usable (the next call starts from a clean state).
+ * Stream-ordered temporaries of a single call are not counted.  No counterpart
+ * in the reference (whose allocation failures exit the process,
+ * src/cuda-common.cuh:67-77). */
+int scd_set_memory_limit(scd_ctx *ctx, uint64_t bytes);
 
 /* Number of kernels this context launched so far (for launch accounting). */
 int scd_kernel_launches(scd_ctx *ctx, uint64_t *count);
@@ -233,6 +240,52 @@ int scd_batch_labels_all(scd_ctx *ctx, uint32_t *labels, uint64_t *vertex_offset
  * candidate. */
 int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t *cta_max, double *best_ms,
                  char *report, uint64_t report_cap);
+
+/* ---- Resident set (continuous batching) ---------------------------------
+ * No counterpart in the reference (one graph per process there).  A context
+ * made a resident set keeps graphs resident on the device and advances every
+ * one of them that is still iterating with the same launches: one step is one
+ * refinement iteration (improve, collect_stats, compute_wcc and the per-graph
+ * loop control of src/main-gpu.cpp:71-95) of all running graphs, replayed from
+ * one captured CUDA graph.  Graphs join between steps: another context converts
+ * them (scd_convert_edges, scd_batch_convert*, or any context with a resident
+ * graph) on its own stream, possibly on another host thread while steps run,
+ * and hands them over with scd_resident_add.  Graphs that stop (converged, or
+ * max_iters reached) leave with scd_resident_take.  Per graph, every result
+ * (labels of every iteration, WCC, iteration count) is identical to running
+ * that graph alone with scd_run; it does not depend on the other graphs or on
+ * when the graph joined. */
+
+/* Makes ctx (its resident graph, if any, is dropped) an empty resident set whose
+ * graphs iterate until wcc < best*(1+threshold) or max_iters iterations. */
+int scd_resident_init(scd_ctx *ctx, double threshold, int max_iters);
+/* Moves every graph resident in src (a plain context or a batch, with or
+ * without labels) into set: src runs the loop's prologue on its own stream
+ * (initial partition unless labels were set, initial WCC), then its device
+ * arrays move to the set, where its graphs join at the next scd_resident_step;
+ * src is left empty and reusable.  ids (nullable) receives one id per graph
+ * (the batch order of src).  May be called from another host thread than the
+ * one stepping the set (one thread per src). */
+int scd_resident_add(scd_ctx *set, scd_ctx *src, uint64_t *ids);
+/* One step: graphs waiting to join are merged in (the union is re-formed, and
+ * also when taken graphs hold more than a quarter of it), then one iteration of
+ * every running graph.  running / finished (nullable): graphs that iterated in
+ * this step (0 if none was running) / graphs that stopped in this step (their
+ * results wait for scd_resident_take; joining empty graphs stop at once). */
+int scd_resident_step(scd_ctx *set, uint32_t *running, uint32_t *finished);
+/* Takes up to cap stopped graphs out of the set: ids[k], results[k] (as
+ * scd_run's, ms_iterations = time since it was handed over) and status[k]
+ * (SCD_OK, or SCD_ERR_LIMIT if max_iters stopped it); labels (nullable) receives
+ * their best labels in their own numbering, graph k at
+ * labels[label_offsets[k] .. label_offsets[k+1]) (label_offsets: cap+1 entries);
+ * graphs are taken while their labels fit in labels_cap entries.  *count: graphs
+ * taken.  Any array but count may be NULL. */
+int scd_resident_take(scd_ctx *set, uint32_t cap, uint64_t *ids, scd_result *results, int32_t *status,
+                      uint32_t *labels, uint64_t labels_cap, uint64_t *label_offsets, uint32_t *count);
+/* graphs held (not yet taken), running, waiting to join; steps made, the sum of
+ * running graphs over the steps (graph-iterations), kernels of the last step. */
+int scd_resident_info(scd_ctx *set, uint32_t *graphs, uint32_t *running, uint32_t *pending, uint64_t *steps,
+                      uint64_t *graph_steps, uint64_t *kernels_per_step);
 
 /* WCC of a labelling without any device allocation.  It has no counterpart in
  * the reference: it exists for callers that cannot let a library call

@@ -165,15 +165,13 @@ def run_case(name, text_path, pairs, manifest, trace=True, start_labels=None):
 
 
 # Full-size workloads pinned by hashes (pins.json): the R-MAT graph of the headline
-# benchmark (scale 22), the skewed-degree Chung-Lu stress graph (8M vertices,
-# hubs to ~82k), and a 2M-vertex Chung-Lu graph whose hubs also pass degree
-# 46,341, where the int32 products of the gain model wrap.
+# benchmark (scale 22) and the skewed-degree Chung-Lu stress graph (8M vertices).
+# Both have vertices of degree > 46,341, where the int32 products of the gain
+# model wrap (max degree 160,369 and 79,126).
 PIN_WORKLOADS = {
     "rmat_22": ("rmat", dict(scale=22, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=22)),
     "chunglu_8m": ("chunglu", dict(n=8_000_000, gamma=2.1, wmin=5.0, wmax=200000.0, mu=0.2, smin=10, smax=500,
                                    seed=3)),
-    "chunglu_2m_hubs": ("chunglu", dict(n=2_000_000, gamma=2.1, wmin=5.0, wmax=200000.0, mu=0.2, smin=10,
-                                        smax=500, seed=3)),
 }
 
 
