@@ -728,8 +728,8 @@ void finish_loaded_graph(Ctx &c, double alpha) {
         throw Error(SCD_ERR_FORMAT, "indices do not match m");
     }
     c.alpha = alpha;
-    c.has_graph = true;
     finish_graph(c);
+    c.has_graph = true;
     CK(cudaStreamSynchronize(c.stream));
 }
 

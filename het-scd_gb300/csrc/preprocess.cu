@@ -514,8 +514,8 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
         sort_rows(c, g.indices, n2, g.adj, false, nullptr, s);
         c.launches++;
     }
-    c.has_graph = true;
     finish_graph(c);
+    c.has_graph = true;   // only once every array exists: a failure above leaves no graph
 }
 
 void alloc_graph(Ctx &c, uint32_t n, uint32_t m) {
@@ -548,8 +548,8 @@ void upload_graph(Ctx &c, uint32_t n, uint32_t m, const uint32_t *indices, const
     } else {
         CK(cudaMemsetAsync(g.indices, 0, ((size_t)n + 1) * 4, s));
     }
-    c.has_graph = true;
     finish_graph(c);
+    c.has_graph = true;
 }
 
 }  // namespace scd

@@ -18,6 +18,7 @@ and of every labelling of its trace, and the exact FP64 values.
 Run in the development container, where the reference sources exist:
     python tests/golden/make_golden.py            # fixtures + manifest.json
     python tests/golden/make_golden.py --pins     # pins.json (reference runs of many minutes)
+    python tests/golden/make_golden.py --cli      # the reference CLIs' stdout lines, into manifest.json
 """
 import hashlib
 import time
@@ -235,7 +236,48 @@ def make_pins(names):
         print(name, json.dumps({k: pins[name][k] for k in ("n", "m", "max_degree", "iters", "reference_seconds")}))
 
 
+def is_timer(line):
+    return line.endswith(" ms") or "lines read so far" in line
+
+
+def record_cli_lines(manifest):
+    """The stdout lines (timer lines dropped) of the reference's `convert` on each
+    case's text and of its `main` (one thread: the canonical WCC sums) on the
+    resulting graph, for the command-line drop-in test."""
+    import scdgen
+    tmpdir = tempfile.mkdtemp()
+    texts = dict(TEXT_CASES)
+    for name, make in generated_cases().items():
+        p = os.path.join(tmpdir, name + ".txt")
+        scdgen.write_text(p, make())
+        texts[name] = p
+    for name in manifest:
+        if name not in texts:
+            continue
+        src = texts[name]
+        if not os.path.exists(src):
+            p = os.path.join(tmpdir, name + ".txt")
+            open(p, "w").write(src)
+            src = p
+        gpath = os.path.join(tmpdir, name + ".graph")
+        conv = subprocess.run([os.path.join(REF, "convert"), src, gpath], capture_output=True, text=True, check=True)
+        lines = [l.replace(src, "<input>").replace(gpath, "<output>") for l in conv.stdout.splitlines()]
+        manifest[name]["ref_convert_lines"] = [l for l in lines if not is_timer(l)]
+        if manifest[name]["n"] > 0:
+            main = subprocess.run([os.path.join(REF, "main"), gpath], capture_output=True, text=True, check=True,
+                                  env=dict(os.environ, OMP_NUM_THREADS="1"))
+            manifest[name]["ref_main_lines"] = [l for l in main.stdout.splitlines() if l and not is_timer(l)]
+        os.unlink(gpath)
+
+
 def main():
+    if "--cli" in sys.argv:
+        mpath = os.path.join(HERE, "manifest.json")
+        manifest = json.load(open(mpath))
+        record_cli_lines(manifest)
+        with open(mpath, "w") as f:
+            json.dump(manifest, f, indent=1, sort_keys=True)
+        return
     if "--pins" in sys.argv:
         names = [a for a in sys.argv[1:] if not a.startswith("--")] or list(PIN_WORKLOADS)
         if not os.path.exists(os.path.join(REF, "ref_driver")):
