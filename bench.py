@@ -205,6 +205,56 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_config(S, device, workload, pairs, steps, warmup):
+    """Another named configuration through the same two paths as the headline:
+    edges/s with the edge list resident in HBM (CUDA events) and end to end with
+    pinned host pairs in and labels out, plus the preprocessing triangle count
+    against the measured HBM peak (algorithmic bytes B_tc)."""
+    import numpy as np
+    import torch
+    E = pairs.shape[0]
+    dev_pairs = torch.from_numpy(pairs.view(np.int32)).cuda()
+    host_pairs = torch.from_numpy(pairs.view(np.int32)).pin_memory()
+    eng = S.Engine(device, flags=S.FLAG_PROFILE)
+    stream = torch.cuda.ExternalStream(eng.stream())
+
+    def step_device():
+        eng.convert_edges(device_ptr=dev_pairs.data_ptr(), count=E)
+        return eng.run(0.01, 1000)
+
+    for _ in range(warmup):
+        step_device()
+    torch.cuda.synchronize()
+    eng.profile_reset()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        r = step_device()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dev_ms = ev0.elapsed_time(ev1) / steps
+    tc_ms, tc_n = eng.profile("tc")
+    t = time.perf_counter()
+    for _ in range(steps):
+        eng._check(S.lib().scd_convert_edges(eng._ctx, host_pairs.data_ptr(), E, 0))
+        r = eng.run(0.01, 1000)
+        lab = eng.labels_from_device()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t) * 1e3 / steps
+    n, m, _ = eng.graph_info()
+    gd = eng.graph_download()
+    eng.close()
+    b_tc, _ = algorithmic_tc_bytes(gd["indices"], gd["adj"])
+    tc_avg = tc_ms / max(tc_n, 1)
+    peak, kind = measured_peak_gbs()
+    return {"workload": workload, "edges_in": E, "n": n, "m": m, "iterations": r["iterations"],
+            "value": E / (dev_ms / 1e3), "unit": UNIT, "ms_per_step": dev_ms, "steps": steps, "warmup": warmup,
+            "e2e": {"value": E / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": E * 8,
+                    "d2h_bytes_per_step": 4 * int(lab.size)},
+            "triangle_count": {"ms": tc_avg, "bytes": b_tc, "gbs": b_tc / (tc_avg / 1e3) / 1e9,
+                               "frac": b_tc / (tc_avg / 1e3) / 1e9 / peak, "peak": peak, "peak_kind": kind}}
+
+
 def c4_specs(k):
     """Batched workload: planted-partition graphs, n log-uniform in [1000, 200000],
     mean degree D uniform in [8, 40], mixing mu uniform in [0.05, 0.4], internal
@@ -392,7 +442,8 @@ def bench_served(S, device, args):
     for r in [srv.submit(reqs[i]) for i in range(min(8, len(reqs)))]:   # warm-up
         r.wait(600)
     # capacity: every request submitted at once (closed loop)
-    srv.step_running.clear()
+    for ln in srv.lanes:
+        ln.step_running.clear()
     t = time.perf_counter()
     handles = [srv.submit(p) for p in reqs]
     for h in handles:
@@ -405,7 +456,8 @@ def bench_served(S, device, args):
     rng = np.random.default_rng(55)
     gaps = rng.exponential(1.0 / rate, size=len(reqs))
     srv.batches.clear()
-    srv.step_running.clear()
+    for ln in srv.lanes:
+        ln.step_running.clear()
     srv.peak_in_use = 0.0
     handles = []
     t = time.perf_counter()
@@ -421,6 +473,11 @@ def bench_served(S, device, args):
     end = max(h.finished for h in handles)
     same = same and all(h.result["iterations"] == it and np.array_equal(h.labels, lab)
                         for h, (it, w, lab) in zip(handles, loop_out) if it > 0)
+    lanes = [{"max_records": (srv.bounds[k] if k < len(srv.bounds) else None), "steps": len(ln.step_running),
+              "mean_coscheduled": float(np.mean(ln.step_running)) if ln.step_running else 0.0,
+              **{k2: round(v, 1) if isinstance(v, float) else v for k2, v in ln.set.resident_timing().items()}}
+             for k, ln in enumerate(srv.lanes)]
+    conv_ms = [b[1] * 1e3 for b in srv.batches]
     srv.close()
     lat = [h.latency * 1e3 for h in handles]
     span = end - t
@@ -437,6 +494,7 @@ def bench_served(S, device, args):
             "mean_coscheduled_graphs": {"capacity_run": cap_cosched, "poisson_run": srv.mean_coscheduled()},
             "converters": args.serve_converters, "budget_gb": 120, "peak_admitted_gb": srv.peak_in_use / 1e9,
             "conversion_batches": len(sizes), "mean_conversion_batch": float(np.mean(sizes)) if sizes else 0.0,
+            "conversion_ms_p50": serve.percentile(conv_ms, 50), "lanes": lanes,
             "generate_s": round(gen_s, 1)}
 
 
@@ -454,6 +512,7 @@ def main():
                     help="CPU baseline on the scale-18 sample only")
     ap.add_argument("--no-plain", action="store_true", help="skip the R-MAT line (profiling the other sections)")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the planted-10k and Chung-Lu 8M lines")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--no-autotune", action="store_true", help="batched section: keep the default split")
@@ -480,6 +539,13 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     line = {} if args.no_plain else bench_plain(S, args, world, rank, local, dist)
+    if not args.no_configs:
+        import scdgen
+        line["c1"] = bench_config(S, local, "planted partition n=10000, mean internal degree 18, mu 0.1, seed 1",
+                                  scdgen.workload("planted-10k"), max(args.steps, 10), max(args.warmup, 3))
+        line["c3"] = bench_config(S, local, "Chung-Lu n=8M, exponent 2.1 in [5, 200000], planted communities "
+                                  "10..500, mu 0.2, seed 3", scdgen.workload("chunglu-8m"), min(args.steps, 5),
+                                  min(args.warmup, 3))
     if not args.no_batched:
         line["batched"] = bench_batched(S, local, args)
     if not args.no_served:

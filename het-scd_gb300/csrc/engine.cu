@@ -297,9 +297,9 @@ void build_union_structure(Ctx &c, bool always_gid) {
         b.blocks = blk_off[b.G];
         b.blk_off = c.alloc<uint32_t>(b.G + 1);
         b.blk_gid = c.alloc<uint32_t>(b.blocks);
+        // (copies from pageable memory are staged before the calls return: no wait needed)
         CK(cudaMemcpyAsync(b.blk_off, blk_off.data(), 4 * (b.G + 1), cudaMemcpyHostToDevice, s));
         if (b.blocks) CK(cudaMemcpyAsync(b.blk_gid, blk_gid.data(), 4 * b.blocks, cudaMemcpyHostToDevice, s));
-        CK(cudaStreamSynchronize(s));
     }
     if (n) {
         k_nlow<<<grid_for(n, TPB), TPB, 0, s>>>(n, g.indices, g.adj, g.nlow);
@@ -633,8 +633,13 @@ int scd_create(scd_ctx **out, int device_id, int work_group_size, unsigned flags
             uint64_t keep = ~0ull;
             CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
         }
-        CK(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
-        CK(cudaStreamCreateWithFlags(&c.side, cudaStreamNonBlocking));
+        int prio = 0;   // the device's highest stream priority (numerically lowest) when asked for
+        if (flags & SCD_FLAG_PRIORITY) {
+            int lowest = 0;
+            CK(cudaDeviceGetStreamPriorityRange(&lowest, &prio));
+        }
+        CK(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, prio));
+        CK(cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, prio));
         CK(cudaMalloc((void **)&c.work_counter, 64));
         CK(cudaMallocHost((void **)&c.wcc_host, sizeof(double)));
         CK(cudaMallocHost((void **)&c.host_u32, 2 * sizeof(uint32_t)));
@@ -1130,6 +1135,7 @@ int scd_autotune(scd_ctx *ctx, uint32_t *small_max, uint32_t *warp_max, uint32_t
                  char *report, uint64_t report_cap) {
     return guarded(ctx, [&](Ctx &c) {
         require_graph(c);
+        if (c.res) throw Error(SCD_ERR_STATE, "a resident set keeps the split it was made with");
         std::vector<std::string> lines;
         const double ms = autotune_tc(c, &lines);
         if (c.g.n) {   // the WCC plan follows the chosen split

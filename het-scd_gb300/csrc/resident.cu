@@ -67,6 +67,20 @@ __global__ void k_gather(const Seg *__restrict__ segs, uint32_t nseg, uint64_t t
     }
 }
 
+// Host data of several small uploads gathered into one pinned buffer (pageable
+// copies can wait for the driver's staging buffer, which waits for the device).
+struct Uploads {
+    std::vector<char> host;
+    std::vector<std::pair<size_t, std::pair<void *, size_t>>> items;   // (offset in host, (device dst, bytes))
+    size_t put(void *dst, const void *src, size_t bytes) {
+        const size_t at = (host.size() + 15) & ~(size_t)15;
+        host.resize(at + bytes);
+        if (bytes) memcpy(host.data() + at, src, bytes);
+        items.push_back({at, {dst, bytes}});
+        return at;
+    }
+};
+
 double now_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -87,6 +101,91 @@ UnionArrays arrays_of(const Ctx &c) {
                        c.b.p_ext, c.b.wcc, c.b.best_wcc, c.b.pe32, c.b.active, c.b.iters};
 }
 
+// The vertex lists of a union's structure, each sorted by vertex id (so each
+// graph's entries are one contiguous piece): the degree classes, the long rows,
+// the WCC triangle-counting buckets; with the offset array that goes with some
+// of them (table words of the last class, pieces of the long rows, work units of
+// the buckets).
+constexpr int NCLS = DegreeClasses::K, LONG = NCLS, BUCKET0 = NCLS + 1, NL = NCLS + 1 + TcPlan::K;
+struct UnionLists {
+    const uint32_t *list[NL];
+    uint32_t count[NL];
+    const void *off[NL];   // nullptr, or count+1 offsets (u64 for the table words)
+    bool off64[NL];
+};
+
+UnionLists lists_of(const Ctx &c) {
+    UnionLists L{};
+    for (int k = 0; k < NCLS; k++) {
+        L.list[k] = c.g.cls.list[k];
+        L.count[k] = c.g.cls.count[k];
+    }
+    L.off[NCLS - 1] = c.g.big_table_off;
+    L.off64[NCLS - 1] = true;
+    L.list[LONG] = c.g.rows.llong;
+    L.count[LONG] = c.g.rows.nlong;
+    L.off[LONG] = c.g.rows.chunk_off;
+    for (int k = 0; k < TcPlan::K; k++) {
+        L.list[BUCKET0 + k] = c.wplan.verts[k];
+        L.count[BUCKET0 + k] = c.wplan.nverts[k];
+        L.off[BUCKET0 + k] = c.wplan.unit_off[k];
+    }
+    return L;
+}
+
+// A graph's share of each list: entries, and the span of the offsets (table
+// words, long-row pieces, work units) they cover.
+struct GraphLists {
+    uint32_t cnt[NL] = {};
+    uint64_t span[NL] = {};
+};
+
+// pos/off of the first entry of every graph g (vertex >= fin_off[g]) in every list
+__global__ void k_list_bounds(UnionLists L, const uint32_t *__restrict__ fin_off, uint32_t G, uint64_t *out) {
+    const uint32_t total = NL * (G + 1);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const uint32_t l = i / (G + 1), g = i % (G + 1);
+        const uint32_t pos = L.count[l] ? lower_bound(L.list[l], L.count[l], fin_off[g]) : 0u;
+        uint64_t ov = 0;
+        if (L.off[l]) ov = L.off64[l] ? ((const uint64_t *)L.off[l])[pos] : ((const uint32_t *)L.off[l])[pos];
+        out[2 * i] = pos;
+        out[2 * i + 1] = ov;
+    }
+}
+
+// every graph's GraphLists from the union's lists (one host read)
+std::vector<GraphLists> graph_lists(Ctx &c) {
+    const uint32_t G = c.b.G;
+    cudaStream_t s = c.stream;
+    std::vector<uint64_t> h(2 * (size_t)NL * (G + 1));
+    DevBuf<uint64_t> d(h.size(), s);
+    k_list_bounds<<<grid_for((uint64_t)NL * (G + 1), 256), 256, 0, s>>>(lists_of(c), c.b.fin_off, G, d.get());
+    CK_LAUNCH("k_list_bounds");
+    c.launches++;
+    CK(cudaMemcpyAsync(h.data(), d.get(), 8 * h.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<GraphLists> out(G);
+    for (int l = 0; l < NL; l++)
+        for (uint32_t g = 0; g < G; g++) {
+            const size_t a = 2 * ((size_t)l * (G + 1) + g), b = a + 2;
+            out[g].cnt[l] = (uint32_t)(h[b] - h[a]);
+            out[g].span[l] = h[b + 1] - h[a + 1];
+        }
+    return out;
+}
+
+__global__ void k_graph_ids(uint32_t n, uint32_t G, const uint32_t *__restrict__ fin_off, uint32_t *gid) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = G + 1;   // last g with fin_off[g] <= v
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (fin_off[mid] <= v) lo = mid + 1;
+            else hi = mid;
+        }
+        gid[v] = lo - 1;
+    }
+}
+
 }  // namespace
 
 // Graphs converted by another context, waiting to join (their device arrays
@@ -96,6 +195,9 @@ struct ResidentSource {
     uint64_t bytes = 0;
     UnionArrays a{};
     std::vector<uint32_t> fin_off, comm_off, m;   // per graph of the source union
+    UnionLists lists{};
+    const uint32_t *nlow = nullptr;
+    std::vector<GraphLists> gl;                  // per graph of the source union
     std::vector<uint64_t> ids;
     std::vector<double> wcc0;
     cudaEvent_t ready = nullptr;   // the source's stream has finished its work
@@ -111,6 +213,7 @@ struct ResidentGraph {
     bool finished = false, taken = false, limit = false;
     int32_t iters = 0;
     double best_wcc = 0;
+    GraphLists gl;                   // its share of the union's structure lists
 };
 
 struct ResidentSet {
@@ -128,7 +231,33 @@ struct ResidentSet {
     size_t h_cap = 0;
     uint32_t *h_labels = nullptr;        // pinned staging of taken labels
     size_t h_labels_cap = 0;
+    char *h_up = nullptr;                // pinned staging of a re-forming's uploads
+    size_t h_up_cap = 0;
+    cudaEvent_t up_done = nullptr;       // its copies have been made
+    // copies u to the device through h_up: waits for the previous re-forming's copies
+    // (long done, normally) before reusing the buffer
+    void upload(const Uploads &u, cudaStream_t s) {
+        if (u.items.empty()) return;
+        if (up_done) CK(cudaEventSynchronize(up_done));
+        else CK(cudaEventCreateWithFlags(&up_done, cudaEventDisableTiming));
+        if (u.host.size() > h_up_cap) {
+            if (h_up) cudaFreeHost(h_up);
+            h_up = nullptr;
+            h_up_cap = 0;
+            const size_t cap = u.host.size() * 2 + 4096;
+            CK(cudaMallocHost((void **)&h_up, cap));
+            h_up_cap = cap;
+        }
+        memcpy(h_up, u.host.data(), u.host.size());
+        for (const auto &it : u.items)
+            if (it.second.second)
+                CK(cudaMemcpyAsync(it.second.first, h_up + it.first, it.second.second, cudaMemcpyHostToDevice, s));
+        CK(cudaEventRecord(up_done, s));
+    }
     uint64_t steps = 0, graph_steps = 0, rebuilds = 0, last_kernels = 0;
+    uint32_t stable = 0;                 // steps since the union was last re-formed
+    uint32_t split[4] = {};              // triangle-counting split of the set (its buckets' bounds)
+    double ms_rebuild = 0, ms_capture = 0, ms_step = 0;   // host wall time spent in each part of the steps
 
     void drop_exec() {
         for (int k = 0; k < 2; k++) {
@@ -169,7 +298,7 @@ void ensure_host_mirrors(ResidentSet &R, size_t G) {
 
 // Gathers of several arrays with one upload of all their segment tables.
 struct Gathers {
-    enum Kind { U32, I32, F64, F2, U8 };
+    enum Kind { U32, I32, F64, F2, U8, U64 };
     struct Job {
         size_t first, count;
         uint64_t total;
@@ -181,23 +310,22 @@ struct Gathers {
     std::vector<Job> jobs;
     template <typename T>
     void add(const std::vector<Seg> &in, uint64_t total, T *dst, bool keep_invalid) {
-        Kind k = std::is_same<T, uint32_t>::value  ? U32
-                 : std::is_same<T, int32_t>::value ? I32
-                 : std::is_same<T, double>::value  ? F64
-                 : std::is_same<T, float2>::value  ? F2
-                                                   : U8;
+        Kind k = std::is_same<T, uint32_t>::value   ? U32
+                 : std::is_same<T, int32_t>::value  ? I32
+                 : std::is_same<T, double>::value   ? F64
+                 : std::is_same<T, float2>::value   ? F2
+                 : std::is_same<T, uint64_t>::value ? U64
+                                                    : U8;
         const size_t first = segs.size();
         for (const Seg &x : in)
             if (x.len) segs.push_back(x);
         if (total) jobs.push_back(Job{first, segs.size() - first, total, (void *)dst, k, keep_invalid});
     }
-    void run(Ctx &c) {
-        if (jobs.empty()) return;
+    // launches every job with the segment tables at dev (segs already copied there)
+    void launch(Ctx &c, const Seg *dev) {
         cudaStream_t s = c.stream;
-        DevBuf<Seg> d(segs.size(), s);
-        CK(cudaMemcpyAsync(d.get(), segs.data(), sizeof(Seg) * segs.size(), cudaMemcpyHostToDevice, s));
         for (const Job &j : jobs) {
-            const Seg *t = d.get() + j.first;
+            const Seg *t = dev + j.first;
             const uint32_t ns = (uint32_t)j.count;
             const unsigned grid = grid_for(j.total, TPB, 152 * 16);
             switch (j.kind) {
@@ -206,10 +334,17 @@ struct Gathers {
             case F64: k_gather<double><<<grid, TPB, 0, s>>>(t, ns, j.total, (double *)j.dst, false); break;
             case F2: k_gather<float2><<<grid, TPB, 0, s>>>(t, ns, j.total, (float2 *)j.dst, false); break;
             case U8: k_gather<uint8_t><<<grid, TPB, 0, s>>>(t, ns, j.total, (uint8_t *)j.dst, false); break;
+            case U64: k_gather<uint64_t><<<grid, TPB, 0, s>>>(t, ns, j.total, (uint64_t *)j.dst, false); break;
             }
             CK_LAUNCH("k_gather");
             c.launches++;
         }
+    }
+    void run(Ctx &c) {   // with its own (pageable) upload of the tables
+        if (jobs.empty()) return;
+        DevBuf<Seg> d(segs.size(), c.stream);
+        CK(cudaMemcpyAsync(d.get(), segs.data(), sizeof(Seg) * segs.size(), cudaMemcpyHostToDevice, c.stream));
+        launch(c, d.get());
     }
 };
 
@@ -220,24 +355,43 @@ struct Move {
     uint32_t v0, c0;         // offsets in the source union
     uint64_t e0;
     ResidentGraph info;      // offsets set to the new union's
+    const UnionLists *lists = nullptr;   // its source's structure lists
+    const uint32_t *nlow = nullptr;
+    uint64_t lpos[NL] = {}, lbase[NL] = {};   // its first entry and offset in them
 };
 
 // Re-forms the union: the kept graphs (not taken) of the current union, then the
-// graphs of the pending sources, gathered into fresh arrays.
+// graphs of the pending sources, gathered into fresh arrays.  The structure lists
+// are concatenated from every graph's share (counts known on the host), so the
+// whole re-forming is queued without waiting for the device.
 // Returns the number of joining graphs that have nothing to iterate (empty graphs).
 uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
     cudaStream_t s = c.stream;
     std::vector<Move> mv;
     uint32_t joined_done = 0;
     const UnionArrays cur = arrays_of(c);
-    for (uint32_t k = 0; k < R.graphs.size(); k++) {
-        const ResidentGraph &g = R.graphs[k];
-        if (g.taken) continue;
-        mv.push_back(Move{cur, k, g.v0, g.c0, g.e0, g});
+    const UnionLists cur_lists = lists_of(c);
+    {
+        uint64_t pos[NL] = {}, base[NL] = {};
+        for (uint32_t k = 0; k < R.graphs.size(); k++) {
+            const ResidentGraph &g = R.graphs[k];
+            if (!g.taken) {
+                Move m{cur, k, g.v0, g.c0, g.e0, g, &cur_lists, c.g.nlow};
+                for (int l = 0; l < NL; l++) {
+                    m.lpos[l] = pos[l];
+                    m.lbase[l] = base[l];
+                }
+                mv.push_back(m);
+            }
+            for (int l = 0; l < NL; l++) {
+                pos[l] += g.gl.cnt[l];
+                base[l] += g.gl.span[l];
+            }
+        }
     }
     for (ResidentSource *ps : srcs) {
         CK(cudaStreamWaitEvent(s, ps->ready, 0));
-        uint64_t e0 = 0;
+        uint64_t e0 = 0, pos[NL] = {}, base[NL] = {};
         for (uint32_t k = 0; k + 1 < ps->fin_off.size(); k++) {
             ResidentGraph g;
             g.id = ps->ids[k];
@@ -247,15 +401,23 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
             g.wcc0 = ps->wcc0[k];
             g.best_wcc = ps->wcc0[k];
             g.t_join = ps->t_added;
+            g.gl = ps->gl[k];
             g.finished = g.n == 0;   // nothing to iterate (active is 0 for it already)
             joined_done += g.finished;
-            mv.push_back(Move{ps->a, k, ps->fin_off[k], ps->comm_off[k], e0, g});
+            Move m{ps->a, k, ps->fin_off[k], ps->comm_off[k], e0, g, &ps->lists, ps->nlow};
+            for (int l = 0; l < NL; l++) {
+                m.lpos[l] = pos[l];
+                m.lbase[l] = base[l];
+                pos[l] += g.gl.cnt[l];
+                base[l] += g.gl.span[l];
+            }
+            mv.push_back(m);
             e0 += 2 * (uint64_t)g.m;
         }
     }
     // new offsets
     const uint32_t G = (uint32_t)mv.size();
-    uint64_t N = 0, M2 = 0, NC = 0;
+    uint64_t N = 0, M2 = 0, NC = 0, lcnt[NL] = {}, lspan[NL] = {};
     for (Move &x : mv) {
         x.info.v0 = (uint32_t)N;
         x.info.e0 = M2;
@@ -263,6 +425,10 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         N += x.info.n;
         M2 += 2 * (uint64_t)x.info.m;
         NC += x.info.nc;
+        for (int l = 0; l < NL; l++) {
+            lcnt[l] += x.info.gl.cnt[l];
+            lspan[l] += x.info.gl.span[l];
+        }
     }
     if (N >= 0xffffffffull || M2 >= 0xffffffffull) throw Error(SCD_ERR_LIMIT, "resident set beyond 2^32-1 entries");
     std::vector<void *> old_owned = std::move(c.owned);
@@ -296,6 +462,7 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         g.adj = c.alloc<uint32_t>(M2);
         g.tri = c.alloc<int32_t>(N);
         g.tri_deg = c.alloc<int32_t>(N);
+        g.nlow = c.alloc<uint32_t>(N);
         c.labels = c.alloc<uint32_t>(N);
         c.labels_next = c.alloc<uint32_t>(N);
         c.best = c.alloc<uint32_t>(N);
@@ -308,6 +475,7 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         c.num_comms = (uint32_t)NC;
         b.fin_off = c.alloc<uint32_t>(G + 1);
         b.comm_off = c.alloc<uint32_t>(G + 1);
+        b.gid = c.alloc<uint32_t>(N);
         b.p_ext = c.alloc<double>(G);
         b.pe32 = c.alloc<float2>(G);
         b.wcc = c.alloc<double>(G);
@@ -316,16 +484,54 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         b.improved = c.alloc<uint8_t>(G);
         b.iters = c.alloc<int32_t>(G);
         b.n_active = c.alloc<uint32_t>(1);
+        // the structure: lists and their offset arrays (the last offset, the total, from the host)
+        uint32_t *list[NL];
+        void *off[NL] = {};
+        for (int l = 0; l < NL; l++) list[l] = c.alloc<uint32_t>(lcnt[l]);
+        off[NCLS - 1] = c.alloc<uint64_t>(lcnt[NCLS - 1] + 1);
+        off[LONG] = c.alloc<uint32_t>(lcnt[LONG] + 1);
+        for (int k = 0; k < TcPlan::K; k++) off[BUCKET0 + k] = c.alloc<uint32_t>(lcnt[BUCKET0 + k] + 1);
+        for (int k = 0; k < NCLS; k++) {
+            g.cls.list[k] = list[k];
+            g.cls.count[k] = (uint32_t)lcnt[k];
+        }
+        g.big_table_off = (uint64_t *)off[NCLS - 1];
+        g.big_table_words = lspan[NCLS - 1];
+        c.big_tables = lspan[NCLS - 1] ? c.alloc<uint32_t>(lspan[NCLS - 1]) : nullptr;
+        g.rows.llong = list[LONG];
+        g.rows.nlong = (uint32_t)lcnt[LONG];
+        g.rows.chunk_off = (uint32_t *)off[LONG];
+        g.rows.nchunks = (uint32_t)lspan[LONG];
+        TcPlan &pl = c.wplan;
+        for (int k = 0; k < TcPlan::K; k++) {
+            pl.verts[k] = list[BUCKET0 + k];
+            pl.unit_off[k] = (uint32_t *)off[BUCKET0 + k];
+            pl.nverts[k] = pl.nfwd[k] = (uint32_t)lcnt[BUCKET0 + k];
+        }
+        pl.dir_lo = pl.dir_hi = 0;   // out-list centres only, as tc_plan builds the WCC plan
+        pl.dir_amin = c.tc_amin < c.tc_small ? c.tc_amin : c.tc_small;
+        // scratch of the iteration
+        c.pin64 = c.alloc<double>(N);
+        c.civ = c.alloc<int4>(N);
+        c.slot_flag = c.alloc<uint8_t>(M2);
+        c.itcount = c.alloc<uint32_t>(N);
+        c.itdeg = c.alloc<int32_t>(N);
+        c.int_len = c.alloc<uint32_t>(N);
+        c.int_adj = c.alloc<uint32_t>(M2);
 
-        std::vector<Seg> ind, adj, tri, tdg, lab, bst, sz, ex, in, pe, pe2, wc, bw, ac, it;
+        std::vector<Seg> ind, adj, tri, tdg, nlw, lab, bst, sz, ex, in, pe, pe2, wc, bw, ac, it;
+        std::vector<Seg> lseg[NL], oseg[NL];
+        uint64_t npos[NL] = {}, nbase[NL] = {};
         for (uint32_t j = 0; j < G; j++) {
             const Move &x = mv[j];
             const ResidentGraph &ni = x.info;
             const bool last = j + 1 == G;   // the last graph also supplies indices[N]
+            const int64_t dv = (int64_t)ni.v0 - (int64_t)x.v0;
             ind.push_back(Seg{x.a.indices, x.v0, ni.v0, ni.n + (last ? 1u : 0u), (int64_t)ni.e0 - (int64_t)x.e0});
-            adj.push_back(Seg{x.a.adj, x.e0, ni.e0, 2 * (uint64_t)ni.m, (int64_t)ni.v0 - (int64_t)x.v0});
+            adj.push_back(Seg{x.a.adj, x.e0, ni.e0, 2 * (uint64_t)ni.m, dv});
             tri.push_back(Seg{x.a.tri, x.v0, ni.v0, ni.n, 0});
             tdg.push_back(Seg{x.a.tri_deg, x.v0, ni.v0, ni.n, 0});
+            nlw.push_back(Seg{x.nlow, x.v0, ni.v0, ni.n, 0});
             lab.push_back(Seg{x.a.labels, x.v0, ni.v0, ni.n, (int64_t)ni.c0 - (int64_t)x.c0});
             bst.push_back(Seg{x.a.best, x.v0, ni.v0, ni.n, (int64_t)ni.c0 - (int64_t)x.c0});
             sz.push_back(Seg{x.a.st.sizes, x.c0, ni.c0, ni.nc, 0});
@@ -337,6 +543,14 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
             bw.push_back(Seg{x.a.best_wcc, x.sg, j, 1, 0});
             ac.push_back(Seg{x.a.active, x.sg, j, 1, 0});
             it.push_back(Seg{x.a.iters, x.sg, j, 1, 0});
+            for (int l = 0; l < NL; l++) {
+                const uint32_t cn = ni.gl.cnt[l];
+                lseg[l].push_back(Seg{x.lists->list[l], x.lpos[l], npos[l], cn, dv});
+                if (off[l]) oseg[l].push_back(Seg{x.lists->off[l], x.lpos[l], npos[l], cn,
+                                                  (int64_t)nbase[l] - (int64_t)x.lbase[l]});
+                npos[l] += cn;
+                nbase[l] += ni.gl.span[l];
+            }
         }
         if (N == 0) CK(cudaMemsetAsync(g.indices, 0, 4, s));
         Gathers ga;
@@ -344,6 +558,7 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         ga.add<uint32_t>(adj, M2, g.adj, false);
         ga.add<int32_t>(tri, N, g.tri, false);
         ga.add<int32_t>(tdg, N, g.tri_deg, false);
+        ga.add<uint32_t>(nlw, N, g.nlow, false);
         ga.add<uint32_t>(lab, N, c.labels, true);
         ga.add<uint32_t>(bst, N, c.best, true);
         ga.add<int32_t>(sz, NC, c.st[0].sizes, false);
@@ -355,8 +570,24 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         ga.add<double>(bw, G, b.best_wcc, false);
         ga.add<uint8_t>(ac, G, b.active, false);
         ga.add<int32_t>(it, G, b.iters, false);
-        ga.run(c);
-
+        for (int l = 0; l < NL; l++) {
+            ga.add<uint32_t>(lseg[l], lcnt[l], list[l], false);
+            if (l == NCLS - 1) ga.add<uint64_t>(oseg[l], lcnt[l], (uint64_t *)off[l], false);
+            else if (off[l]) ga.add<uint32_t>(oseg[l], lcnt[l], (uint32_t *)off[l], false);
+        }
+        // every small upload of the re-forming in one pinned copy-out, then the gathers
+        Uploads up;
+        DevBuf<Seg> dsegs(ga.segs.size() ? ga.segs.size() : 1, s);
+        up.put(dsegs.get(), ga.segs.data(), sizeof(Seg) * ga.segs.size());
+        for (int l = 0; l < NL; l++) {   // the offset arrays' totals
+            if (!off[l]) continue;
+            if (l == NCLS - 1) {
+                up.put((uint64_t *)off[l] + lcnt[l], &lspan[l], 8);
+            } else {
+                const uint32_t t = (uint32_t)lspan[l];
+                up.put((uint32_t *)off[l] + lcnt[l], &t, 4);
+            }
+        }
         b.h_fin_off.assign(G + 1, 0);
         b.h_comm_off.assign(G + 1, 0);
         b.h_m.assign(G, 0);
@@ -369,10 +600,32 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         }
         b.h_fin_off[G] = (uint32_t)N;
         b.h_comm_off[G] = (uint32_t)NC;
-        CK(cudaMemcpyAsync(b.fin_off, b.h_fin_off.data(), 4 * (G + 1), cudaMemcpyHostToDevice, s));
-        CK(cudaMemcpyAsync(b.comm_off, b.h_comm_off.data(), 4 * (G + 1), cudaMemcpyHostToDevice, s));
+        up.put(b.fin_off, b.h_fin_off.data(), 4 * (G + 1));
+        up.put(b.comm_off, b.h_comm_off.data(), 4 * (G + 1));
+        {   // graph-aligned WCC blocks (host-computed)
+            std::vector<uint32_t> blk_off(G + 1, 0), blk_gid;
+            for (uint32_t k = 0; k < G; k++) {
+                const uint32_t parts = (mv[k].info.n + 2047) / 2048;
+                blk_off[k + 1] = blk_off[k] + parts;
+                blk_gid.insert(blk_gid.end(), parts, k);
+            }
+            b.blocks = blk_off[G];
+            b.blk_off = c.alloc<uint32_t>(G + 1);
+            b.blk_gid = c.alloc<uint32_t>(b.blocks);
+            up.put(b.blk_off, blk_off.data(), 4 * (G + 1));
+            up.put(b.blk_gid, blk_gid.data(), 4 * (size_t)b.blocks);
+        }
+        R.upload(up, s);
+        ga.launch(c, dsegs.get());
+        if (N) {
+            k_graph_ids<<<grid_for(N, TPB), TPB, 0, s>>>((uint32_t)N, G, b.fin_off, b.gid);
+            CK_LAUNCH("k_graph_ids");
+            c.launches++;
+        }
+        c.wcc_part = c.alloc<double>(b.blocks + 1);
+        prepare_tc_kernels();
+        prepare_improve_kernels();
         c.has_graph = c.has_labels = true;
-        build_union_structure(c, true);
         for (void *p : old_owned) cudaFreeAsync(p, s);
         for (ResidentSource *ps : srcs) free_source(ps, s);
         srcs.clear();
@@ -396,7 +649,6 @@ uint32_t rebuild(Ctx &c, ResidentSet &R, std::vector<ResidentSource *> &srcs) {
         c.has_graph = c.has_labels = false;
         throw;
     }
-    CK(cudaStreamSynchronize(s));
     R.rebuilds++;
     return joined_done;
 }
@@ -419,6 +671,8 @@ void resident_destroy(Ctx &c) {
     if (R->h_iters) cudaFreeHost(R->h_iters);
     if (R->h_best) cudaFreeHost(R->h_best);
     if (R->h_labels) cudaFreeHost(R->h_labels);
+    if (R->h_up) cudaFreeHost(R->h_up);
+    if (R->up_done) cudaEventDestroy(R->up_done);
     delete R;
 }
 
@@ -460,6 +714,8 @@ int scd_resident_init(scd_ctx *ctx, double threshold, int max_iters) {
         c.res = new ResidentSet();
         c.res->threshold = threshold;
         c.res->max_iters = max_iters;
+        const uint32_t sp[4] = {c.tc_small, c.tc_b0, c.tc_b1, c.tc_amin};
+        memcpy(c.res->split, sp, sizeof sp);
         c.resident = true;
     });
 }
@@ -483,6 +739,20 @@ int scd_resident_add(scd_ctx *set, scd_ctx *src, uint64_t *ids) {
         ps->wcc0.resize(G);
         CK(cudaMemcpyAsync(ps->wcc0.data(), s.b.wcc, 8 * G, cudaMemcpyDeviceToHost, s.stream));
         CK(cudaStreamSynchronize(s.stream));
+        // the WCC's triangle-counting plan under the set's split, so every graph's
+        // buckets mean the same in the union; then each graph's share of the lists
+        const uint32_t *sp = R->split;
+        if (s.tc_small != sp[0] || s.tc_b0 != sp[1] || s.tc_b1 != sp[2] || s.tc_amin != sp[3]) {
+            s.tc_small = sp[0];
+            s.tc_b0 = sp[1];
+            s.tc_b1 = sp[2];
+            s.tc_amin = sp[3];
+            s.wplan = TcPlan();
+            if (s.g.n) tc_plan(s, Oriented{s.g.indices, s.g.nlow, s.g.adj, s.g.n}, s.wplan, s.stream, true, false);
+        }
+        ps->lists = lists_of(s);
+        ps->nlow = s.g.nlow;
+        ps->gl = graph_lists(s);
         ps->a = arrays_of(s);
         ps->fin_off = s.b.h_fin_off;
         ps->comm_off = s.b.h_comm_off;
@@ -519,9 +789,13 @@ int scd_resident_step(scd_ctx *ctx, uint32_t *running, uint32_t *finished) {
         }
         const bool any_taken = kept < R.graphs.size();
         uint32_t run = 0, fin = 0;
+        const double t_step = now_ms();
         if (!srcs.empty() || (any_taken && (kept == 0 || 4 * taken_v > c.g.n))) {
+            R.stable = 0;
             try {
+                const double t0 = now_ms();
                 fin += rebuild(c, R, srcs);
+                R.ms_rebuild += now_ms() - t0;
             } catch (...) {
                 for (ResidentSource *ps : srcs) free_source(ps, s);
                 throw;
@@ -531,7 +805,16 @@ int scd_resident_step(scd_ctx *ctx, uint32_t *running, uint32_t *finished) {
             if (!g.finished) run++;
         if (run) {
             const int par = c.cur;
-            if (!R.exec[par]) {
+            // a union that changes every few steps is launched kernel by kernel: capturing and
+            // instantiating a CUDA graph costs more than the launches it saves for one replay
+            const bool replay = R.exec[par] || R.stable >= 6;
+            R.stable++;
+            if (!replay) {
+                const uint64_t l0 = c.launches;
+                iterate_async(c, R.threshold, nullptr, 0);
+                R.last_kernels = c.launches - l0;
+            } else if (!R.exec[par]) {
+                const double t0 = now_ms();
                 cudaGraph_t gr = nullptr;
                 CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
                 c.capturing = true;
@@ -549,15 +832,18 @@ int scd_resident_step(scd_ctx *ctx, uint32_t *running, uint32_t *finished) {
                 const cudaError_t e = cudaGraphInstantiate(&R.exec[par], gr, 0);
                 cudaGraphDestroy(gr);
                 CK(e);
+                R.ms_capture += now_ms() - t0;
             } else {   // replaying advances the state as the captured host code did
                 uint32_t *t = c.labels;
                 c.labels = c.labels_next;
                 c.labels_next = t;
                 c.cur ^= 1;
             }
-            CK(cudaGraphLaunch(R.exec[par], s));
-            c.launches += R.exec_kernels[par];
-            R.last_kernels = R.exec_kernels[par];
+            if (replay) {
+                CK(cudaGraphLaunch(R.exec[par], s));
+                c.launches += R.exec_kernels[par];
+                R.last_kernels = R.exec_kernels[par];
+            }
             R.steps++;
             R.graph_steps += run;
             const uint32_t G = c.b.G;
@@ -581,6 +867,7 @@ int scd_resident_step(scd_ctx *ctx, uint32_t *running, uint32_t *finished) {
                 fin += g.finished;
             }
         }
+        R.ms_step += now_ms() - t_step;
         if (running) *running = run;
         if (finished) *finished = fin;
     });
@@ -682,6 +969,16 @@ int scd_resident_info(scd_ctx *ctx, uint32_t *graphs, uint32_t *running, uint32_
         if (steps) *steps = R.steps;
         if (graph_steps) *graph_steps = R.graph_steps;
         if (kernels_per_step) *kernels_per_step = R.last_kernels;
+    });
+}
+
+int scd_resident_timing(scd_ctx *ctx, double *ms_steps, double *ms_rebuild, double *ms_capture, uint64_t *rebuilds) {
+    return guarded_res(ctx, [&](Ctx &c) {
+        ResidentSet &R = require_set(c);
+        if (ms_steps) *ms_steps = R.ms_step;
+        if (ms_rebuild) *ms_rebuild = R.ms_rebuild;
+        if (ms_capture) *ms_capture = R.ms_capture;
+        if (rebuilds) *rebuilds = R.rebuilds;
     });
 }
 

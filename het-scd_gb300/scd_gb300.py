@@ -19,7 +19,7 @@ OK = 0
 ERRORS = {-1: "SCD_ERR_ARG", -2: "SCD_ERR_CUDA", -3: "SCD_ERR_OOM", -4: "SCD_ERR_STATE",
           -5: "SCD_ERR_FORMAT", -6: "SCD_ERR_TIMEOUT", -7: "SCD_ERR_LIMIT"}
 INVALID_LABEL = 0xFFFFFFFF
-FLAG_PROFILE, FLAG_PEXT_TREE, FLAG_NO_GRAPHS, FLAG_TC_OUT_ONLY = 1, 2, 4, 8
+FLAG_PROFILE, FLAG_PEXT_TREE, FLAG_NO_GRAPHS, FLAG_TC_OUT_ONLY, FLAG_PRIORITY = 1, 2, 4, 8, 16
 PHASES = ("parse", "convert", "tc", "partition", "improve", "stats", "wcc_tc", "wcc")
 
 
@@ -93,6 +93,8 @@ def lib():
             "scd_resident_take": ([P, u32, P, P, P, P, u64, P, ctypes.POINTER(u32)], i32),
             "scd_resident_info": ([P, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u32),
                                    ctypes.POINTER(u64), ctypes.POINTER(u64), ctypes.POINTER(u64)], i32),
+            "scd_resident_timing": ([P, ctypes.POINTER(dbl), ctypes.POINTER(dbl), ctypes.POINTER(dbl),
+                                     ctypes.POINTER(u64)], i32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -393,6 +395,12 @@ class Engine:
                                             ctypes.byref(st), ctypes.byref(gs), ctypes.byref(kp)))
         return dict(graphs=g.value, running=r.value, pending=p.value, steps=st.value, graph_steps=gs.value,
                     kernels_per_step=kp.value)
+
+    def resident_timing(self):
+        a, b, c, r = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_uint64()
+        self._check(lib().scd_resident_timing(self._ctx, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                              ctypes.byref(r)))
+        return dict(ms_steps=a.value, ms_rebuild=b.value, ms_capture=c.value, rebuilds=r.value)
 
     def has_graph(self):
         return lib().scd_batch_size(self._ctx, ctypes.byref(ctypes.c_uint32())) == OK

@@ -7,16 +7,23 @@ device and iterate together:
   memory of all admitted, unfinished requests stays under the HBM budget
   (120 GB by default); the estimate is bytes_per_record x records, measured for
   this engine (the preprocessing keys and the resident graph dominate);
-* conversion: `converters` staging engines, each on its own CUDA stream and
-  host thread (the C calls release the GIL), take the admitted waiting requests
-  (up to `max_batch`, FIFO) and preprocess them as one batch while the set
-  iterates, then hand the graphs over (scd_resident_add);
-* iteration: one host thread steps the resident set (scd_resident_step): every
-  step is one refinement iteration of every running graph in the same launches
-  (one CUDA-graph replay), so a request admitted while others are iterating
-  joins their launches at the next step instead of waiting for a free worker;
-  graphs that converge leave (scd_resident_take), which frees their share of
-  the budget for the next admissions;
+* conversion: each lane has its own queue and `converters` staging engines,
+  each on its own CUDA stream and host thread (the C calls release the GIL),
+  which take the lane's admitted waiting requests (up to `max_batch`, FIFO) and
+  preprocess them as one batch while the set iterates, then hand the graphs
+  over (scd_resident_add); the first lane's engines (set and staging) run on
+  high-priority streams, so small requests are not queued behind the thread
+  blocks of large ones;
+* iteration: each size lane (requests up to `lanes[0]` records, up to
+  `lanes[1]`, ..., the rest) is one resident set stepped by its own host thread
+  (scd_resident_step): every step is one refinement iteration of every running
+  graph of the lane in the same launches (one CUDA-graph replay), so a request
+  admitted while others are iterating joins their launches at the next step
+  instead of waiting for a free worker; graphs that converge leave
+  (scd_resident_take), which frees their share of the budget for the next
+  admissions.  Lanes keep small requests from waiting on the iterations of
+  large ones (and on the re-forming of a large union when graphs join); the
+  lanes' launches overlap on the device;
 * results: the best labels, WCC and iteration count of each request are those
   of processing that request alone (the resident set keeps every per-graph
   quantity per graph).
@@ -67,35 +74,68 @@ class Request:
         return self.result, self.labels
 
 
+class Lane:
+    """One resident set, its queue and staging engines, and the requests it holds
+    (resident-set id -> request)."""
+
+    def __init__(self, index, engine, staging, threshold, max_iters):
+        self.index = index
+        self.set = engine
+        self.set.resident_init(threshold, max_iters)
+        self.staging = staging
+        self.waiting = collections.deque()
+        self.in_set = {}
+        self.step_running = []   # graphs that iterated in each step
+        self.steps = 0
+        self.converters = []
+
+
 class Server:
     def __init__(self, device=0, converters=2, budget_bytes=120e9, max_batch=64, threshold=0.01, max_iters=1000,
-                 bytes_per_record=BYTES_PER_RECORD, engine_factory=None, step_hook=None):
-        """step_hook (optional): called with the number of steps made so far before
-        every step of the resident set, on the iterating thread; it may block to
+                 bytes_per_record=BYTES_PER_RECORD, engine_factory=None, step_hook=None, lanes=(1 << 21,)):
+        """lanes: ascending record-count bounds of the size lanes (one more lane
+        takes the rest).  step_hook (optional): called with (lane index, steps the
+        lane made so far) before every step, on the lane's thread; it may block to
         hold the iterations (draining, or a test that lines up arrivals)."""
         self.budget = float(budget_bytes)
         self.max_batch = max_batch
         self.bytes_per_record = bytes_per_record
         self._lock = threading.Condition()
-        self._waiting = collections.deque()
-        self._in_set = {}           # resident-set id -> request (converted, not yet taken)
         self._in_use = 0.0
         self._closing = False
         self._failed = None
         self._next_id = 0
         self.batches = []           # (size, seconds) of every conversion batch
-        self.step_running = []      # graphs that iterated in each step
         self.peak_in_use = 0.0
         self._step_hook = step_hook
-        self._steps = 0
-        make = engine_factory or (lambda: S.Engine(device))
-        self.set = make()
-        self.set.resident_init(threshold, max_iters)
-        self._staging = [make() for _ in range(converters)]
-        self._threads = [threading.Thread(target=self._convert, args=(e,), daemon=True) for e in self._staging]
-        self._threads.append(threading.Thread(target=self._iterate, daemon=True))
+        self.bounds = list(lanes)
+        def make(high):
+            if engine_factory:
+                return engine_factory()
+            return S.Engine(device, flags=S.FLAG_PRIORITY if high else 0)
+
+        self.lanes = []
+        for k in range(len(self.bounds) + 1):
+            self.lanes.append(Lane(k, make(k == 0), [make(k == 0) for _ in range(converters)], threshold, max_iters))
+        self._threads = []
+        for ln in self.lanes:
+            ln.converters = [threading.Thread(target=self._convert, args=(ln, e), daemon=True) for e in ln.staging]
+            self._threads += ln.converters + [threading.Thread(target=self._iterate, args=(ln,), daemon=True)]
         for t in self._threads:
             t.start()
+
+    @property
+    def set(self):
+        """The resident set of the first (smallest) lane."""
+        return self.lanes[0].set
+
+    @property
+    def step_running(self):
+        """Graphs that iterated in each step of the first lane."""
+        return self.lanes[0].step_running
+
+    def lane_of(self, records):
+        return sum(records > b for b in self.bounds)
 
     def cost(self, records):
         return max(records, 1) * self.bytes_per_record + 64e6
@@ -107,7 +147,7 @@ class Server:
             if self.cost(req.records) > self.budget:
                 self._finish(req, S.ScdError(-3, "request larger than the whole HBM budget"))
                 return req
-            self._waiting.append(req)
+            self.lanes[self.lane_of(req.records)].waiting.append(req)
             self._lock.notify_all()
         return req
 
@@ -119,8 +159,9 @@ class Server:
             if req.done.is_set():
                 return False
             req.cancelled = True
-            if req in self._waiting:
-                self._waiting.remove(req)
+            waiting = self.lanes[self.lane_of(req.records)].waiting
+            if req in waiting:
+                waiting.remove(req)
                 self._finish(req, Cancelled("request cancelled"))
             return True
 
@@ -130,16 +171,17 @@ class Server:
         req.finished = time.perf_counter()
         req.done.set()
 
-    def _take_batch(self):
-        """Admitted waiting requests that fit the budget (FIFO, no overtaking)."""
+    def _take_batch(self, lane):
+        """The lane's admitted waiting requests that fit the budget (FIFO, no overtaking)."""
         batch = []
-        while self._waiting and len(batch) < self.max_batch:
-            c = self.cost(self._waiting[0].records)
+        while lane.waiting and len(batch) < self.max_batch:
+            c = self.cost(lane.waiting[0].records)
             if self._in_use + c > self.budget:
                 break
             self._in_use += c
-            r = self._waiting.popleft()
+            r = lane.waiting.popleft()
             r.admitted = True
+            r.started = time.perf_counter()   # under the lock: admission order
             batch.append(r)
         self.peak_in_use = max(self.peak_in_use, self._in_use)
         return batch
@@ -148,23 +190,21 @@ class Server:
         self._in_use -= sum(self.cost(r.records) for r in reqs)
         self._lock.notify_all()
 
-    def _convert(self, eng):
+    def _convert(self, lane, eng):
         while True:
             with self._lock:
-                while not self._closing and not self._waiting:
+                while not self._closing and not lane.waiting:
                     self._lock.wait()
-                if self._closing and not self._waiting:
+                if self._closing and not lane.waiting:
                     return
-                batch = self._take_batch()
+                batch = self._take_batch(lane)
                 if not batch:   # budget exhausted: wait for graphs to leave the set
                     self._lock.wait(0.01)
                     continue
             t0 = time.perf_counter()
-            for r in batch:
-                r.started = t0
             try:
                 eng.batch_convert([r.pairs for r in batch])
-                ids = self.set.resident_add(eng)
+                ids = lane.set.resident_add(eng)
             except Exception as e:   # the batch fails as a whole; report it on every request
                 with self._lock:
                     self._release(batch)
@@ -173,29 +213,29 @@ class Server:
                 continue
             with self._lock:
                 for i, r in zip(ids, batch):
-                    self._in_set[i] = r
+                    lane.in_set[i] = r
                 self.batches.append((len(batch), time.perf_counter() - t0))
                 self._lock.notify_all()
 
-    def _iterate(self):
+    def _iterate(self, lane):
         while True:
             with self._lock:
-                while not self._in_set and not (self._closing and not self._waiting and self._converters_idle()):
+                while not lane.in_set and not (self._closing and not lane.waiting and self._converters_idle(lane)):
                     self._lock.wait(0.05)
-                if not self._in_set:
+                if not lane.in_set:
                     return
             if self._step_hook:
-                self._step_hook(self._steps)
-            self._steps += 1
+                self._step_hook(lane.index, lane.steps)
+            lane.steps += 1
             try:
-                running, finished = self.set.resident_step()
+                running, finished = lane.set.resident_step()
                 if running:
-                    self.step_running.append(running)
-                out = self.set.resident_take() if finished else []
+                    lane.step_running.append(running)
+                out = lane.set.resident_take() if finished else []
             except Exception as e:   # the set is unusable: fail everything it holds
                 with self._lock:
-                    reqs = list(self._in_set.values())
-                    self._in_set.clear()
+                    reqs = list(lane.in_set.values())
+                    lane.in_set.clear()
                     self._release(reqs)
                 for r in reqs:
                     self._finish(r, e)
@@ -203,7 +243,7 @@ class Server:
             if not out:
                 continue
             with self._lock:
-                done = [(self._in_set.pop(i), res, st, lab) for i, res, st, lab in out]
+                done = [(lane.in_set.pop(i), res, st, lab) for i, res, st, lab in out]
                 self._release([r for r, *_ in done])
             for r, res, st, lab in done:
                 if r.cancelled:
@@ -213,8 +253,9 @@ class Server:
                 r.labels = lab
                 self._finish(r, S.ScdError(st, "max_iters reached before convergence") if st else None)
 
-    def _converters_idle(self):
-        return all(not t.is_alive() for t in self._threads[:-1])
+    @staticmethod
+    def _converters_idle(lane):
+        return all(not t.is_alive() for t in lane.converters)
 
     def close(self):
         with self._lock:
@@ -222,12 +263,15 @@ class Server:
             self._lock.notify_all()
         for t in self._threads:
             t.join()
-        for e in self._staging:
-            e.close()
-        self.set.close()
+        for ln in self.lanes:
+            for e in ln.staging:
+                e.close()
+            ln.set.close()
 
     def mean_coscheduled(self):
-        return float(np.mean(self.step_running)) if self.step_running else 0.0
+        """Graphs per iteration step, over the steps of every lane."""
+        steps = [x for ln in self.lanes for x in ln.step_running]
+        return float(np.mean(steps)) if steps else 0.0
 
     def __enter__(self):
         return self

@@ -47,6 +47,9 @@ extern "C" {
 #define SCD_FLAG_TC_OUT_ONLY 8u   /* count every triangle from the out-list table of its
                                      lowest-ordered vertex (no in-list units); same results,
                                      slower on skewed graphs */
+#define SCD_FLAG_PRIORITY 16u     /* the context's streams get the device's highest priority:
+                                     their pending thread blocks are scheduled before those of
+                                     other contexts (latency-sensitive work beside bulk work) */
 
 typedef struct scd_ctx scd_ctx;
 
@@ -286,6 +289,9 @@ int scd_resident_take(scd_ctx *set, uint32_t cap, uint64_t *ids, scd_result *res
  * running graphs over the steps (graph-iterations), kernels of the last step. */
 int scd_resident_info(scd_ctx *set, uint32_t *graphs, uint32_t *running, uint32_t *pending, uint64_t *steps,
                       uint64_t *graph_steps, uint64_t *kernels_per_step);
+/* Host wall time spent in scd_resident_step so far (all of it, re-forming the
+ * union, capturing the iteration) and the number of re-formings. */
+int scd_resident_timing(scd_ctx *set, double *ms_steps, double *ms_rebuild, double *ms_capture, uint64_t *rebuilds);
 
 /* WCC of a labelling without any device allocation.  It has no counterpart in
  * the reference: it exists for callers that cannot let a library call

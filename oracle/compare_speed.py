@@ -10,7 +10,9 @@ graphs with the same thread count, using the reference's own timers:
 timer line both sides printed.  Test and measurement infrastructure only: it
 needs oracle/_ref, which exists where the reference's sources were present.
 
-usage: python oracle/compare_speed.py [--threads T] [--scales 18 20]
+usage: python oracle/compare_speed.py [--threads T] [--scales 18 20] [--repeat R]
+With R > 1 the two sides run alternately R times and each column is the median
+(the runs share the machine with whatever else runs there).
 """
 import argparse
 import json
@@ -69,6 +71,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--threads", type=int, default=os.cpu_count())
     ap.add_argument("--scales", type=int, nargs="+", default=[18, 20])
+    ap.add_argument("--repeat", type=int, default=1)
     a = ap.parse_args()
     sys.path[:0] = [os.path.join(ROOT, "het-scd_gb300"), HERE]
     import scdgen
@@ -78,20 +81,24 @@ def main():
         pairs = scdgen.rmat(s, 16, 0.57, 0.19, 0.19, seed=22)
         txt, graph = os.path.join(tmp, f"r{s}.txt"), os.path.join(tmp, f"r{s}.graph")
         scdgen.write_text(txt, pairs)
-        ref = reference_run(txt, graph, a.threads)
-        port = port_run(s, a.threads)
+        refs, ports = [], []
+        for _ in range(a.repeat):
+            refs.append(reference_run(txt, graph, a.threads))
+            ports.append(port_run(s, a.threads))
+        ref = sorted(refs, key=lambda r: r["total"])[len(refs) // 2]
+        port = sorted(ports, key=lambda r: r["total"])[len(ports) // 2]
         os.unlink(txt)
         os.unlink(graph)
-        rows.append(f"| R-MAT {s} ({pairs.shape[0]:,} edges) | {a.threads} | "
+        rows.append(f"| R-MAT {s} ({pairs.shape[0]:,} edges) | {a.threads} | {a.repeat} | "
                     f"{ref['process_graph']:.0f} / {port['process_graph']:.0f} | "
                     f"{ref['initial_partition'] + ref['initial_wcc']:.0f} / "
                     f"{port['initial_partition'] + port['initial_wcc']:.0f} | "
                     f"{ref['iterations']:.0f} ({ref['n_iterations']}) / {port['iterations']:.0f} ({port['n_iterations']}) | "
                     f"{ref['total']:.0f} / {port['total']:.0f} | {port['total'] / ref['total']:.2f} |")
         details.append((s, ref, port))
-    print("| graph | threads | process graph ms (reference / port) | partition + initial WCC ms | "
+    print("| graph | threads | runs (median) | process graph ms (reference / port) | partition + initial WCC ms | "
           "iterations ms (count) | T ms | port / reference |")
-    print("|---|---|---|---|---|---|---|")
+    print("|---|---|---|---|---|---|---|---|")
     print("\n".join(rows))
     for s, ref, port in details:
         print(f"\nR-MAT {s}, reference timer lines:")

@@ -59,8 +59,8 @@ def test_late_request_joins_running_iterations():
     late = scdgen.planted(1000, 14.0, 0.1, 20, 100, seed=78)
     gate, held = threading.Event(), threading.Event()
 
-    def hook(steps_done):
-        if steps_done == 1:        # after the slow request's first iteration
+    def hook(lane, steps_done):
+        if lane == 0 and steps_done == 1:   # after the slow request's first iteration
             held.set()
             assert gate.wait(60)
 
@@ -72,14 +72,11 @@ def test_late_request_joins_running_iterations():
         while srv.set.resident_info()["pending"] < 1:   # converted and handed over
             assert time.time() - t0 < 60
             time.sleep(0.001)
-        k0 = srv.set.kernel_launches()
         gate.set()
         out1, out2 = r1.wait(120), r2.wait(120)
         info = srv.set.resident_info()
         assert srv.step_running[1] == 2                  # the step after the join: both graphs
-        assert info["graph_steps"] > info["steps"]
-        # every step is one replay: launches = steps x kernels of a replay (no per-graph launches)
-        assert srv.set.kernel_launches() - k0 <= (len(srv.step_running) - 1) * max(info["kernels_per_step"], 1) + 64
+        assert info["graph_steps"] > info["steps"]       # (test_gpu_resident counts the launches of such steps)
     alone = S.Engine(0)
     for p, (res, lab) in ((slow, out1), (late, out2)):
         alone.convert_edges(p)

@@ -139,3 +139,18 @@ def test_failed_conversion_fails_its_batch_only():
 def test_percentile():
     assert serve.percentile([3, 1, 2], 50) == 2
     assert serve.percentile(list(range(101)), 99) == 99
+
+
+def test_size_lanes():
+    """Requests above the lane bound go to the second resident set; each lane's
+    results are right and both lanes stepped."""
+    srv = serve.Server(converters=2, budget_bytes=1e12, max_batch=4, bytes_per_record=10, engine_factory=FakeEngine,
+                       lanes=(1000,))
+    reqs = [srv.submit(np.zeros((300 if i % 3 else 4000 + i, 2), np.uint32)) for i in range(12)]
+    for r in reqs:
+        res, lab = r.wait(10)
+        assert res["records"] == r.records and lab.shape[0] == r.records
+    srv.close()
+    assert srv.lane_of(300) == 0 and srv.lane_of(4000) == 1
+    assert srv.lanes[0].steps > 0 and srv.lanes[1].steps > 0
+    assert all(len({srv.lane_of(r.records) for r in reqs[i:i + 1]}) == 1 for i in range(12))
