@@ -312,19 +312,43 @@ def bench_batched(S, device, args):
     sizes = [g.shape[0] for g in graphs]
     records = int(sum(sizes))
     groups = split_batches(sizes, args.batch_records)
+    # the host edge lists live in pinned memory, as a request buffer of a serving host
+    # would: both arms copy them with DMA at full speed.  (From pageable memory the
+    # device reads them through address translation, whose speed drifted down run
+    # after run in one process: 0.64 -> 0.99 s for the same 14.5 GB.)
+    host = torch.empty(2 * records, dtype=torch.int32, pin_memory=True)
+    hv = host.numpy().view(np.uint32)
+    off = 0
+    for i, g in enumerate(graphs):
+        n2 = 2 * g.shape[0]
+        hv[off:off + n2] = g.reshape(-1)
+        graphs[i] = hv[off:off + n2].reshape(-1, 2)
+        off += n2
+    labels_out = torch.empty(records, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     eng = S.Engine(device)
     eng.batch_convert([graphs[i] for i in groups[0]])
     tune = eng.autotune() if not args.no_autotune else {"small_max": None, "warp_max": None, "cta_max": None,
                                                          "in_list_min": None}
 
+    phase = {"convert_s": 0.0, "run_s": 0.0, "labels_s": 0.0}
+
     def run_group(ids):
-        eng.batch_convert([graphs[i] for i in ids])
-        res, rc = eng.batch_run(0.01, 1000)
-        labs = eng.batch_labels_all()
+        t0 = time.perf_counter()
+        eng.batch_convert([graphs[i] for i in ids])        # H2D of the host lists + device preprocessing
+        t1 = time.perf_counter()
+        res, rc = eng.batch_run(0.01, 1000)                 # initial partition + iterations to convergence
+        t2 = time.perf_counter()
+        labs = [x.copy() for x in eng.batch_labels_all(labels_out)]   # best labels D2H (pinned), kept
+        t3 = time.perf_counter()
+        phase["convert_s"] += t1 - t0
+        phase["run_s"] += t2 - t1
+        phase["labels_s"] += t3 - t2
         return res, rc, labs
 
     run_group(groups[0])                    # warm-up (allocator, module load)
     torch.cuda.synchronize()
+    for key in phase:
+        phase[key] = 0.0
     launches0 = eng.kernel_launches()
     t = time.perf_counter()
     results, not_converged = {}, 0
@@ -341,7 +365,8 @@ def bench_batched(S, device, args):
 
     if args.loop_sample <= 0:
         return {"graphs": k, "edges_in": records, "batches": len(groups), "graphs_per_s": k / batch_s,
-                "edges_per_s": records / batch_s, "seconds": batch_s, "gpu_launches": launches}
+                "edges_per_s": records / batch_s, "seconds": batch_s, "gpu_launches": launches,
+                "phases_s": {key: round(v, 4) for key, v in phase.items()}}
     step = max(1, k // args.loop_sample)
     sample = list(range(0, k, step))[: args.loop_sample]
     plain = S.Engine(device)
@@ -368,12 +393,13 @@ def bench_batched(S, device, args):
             "graphs": k, "edges_in": records, "batches": len(groups), "max_records_per_batch": args.batch_records,
             "graphs_per_s": b_gps, "edges_per_s": records / batch_s, "seconds": batch_s,
             "gpu_launches": launches, "peak_engine_bytes": mem, "not_converged_batches": not_converged,
+            "phases_s": {key: round(v, 4) for key, v in phase.items()},
             "per_graph_loop": {"graphs_per_s": l_gps, "edges_per_s": loop_records / loop_s, "sample_graphs": len(sample),
                                "seconds": loop_s},
             "speedup_vs_loop": b_gps / l_gps, "identical_on_sample": bool(same),
             "autotune": {"small_max": tune["small_max"], "warp_max": tune["warp_max"], "cta_max": tune["cta_max"],
                          "in_list_min": tune["in_list_min"]},
-            "timing": "host wall clock, host edge lists in, host labels out", "generate_s": round(gen_s, 1)}
+            "timing": "host wall clock, host edge lists (pinned) in, host labels out", "generate_s": round(gen_s, 1)}
 
 
 def c5_specs(count, seed=5):

@@ -324,12 +324,15 @@ class Engine:
         self._check(lib().scd_batch_labels(self._ctx, g, _p(out)))
         return out[:n]
 
-    def batch_labels_all(self):
-        """Best labels of every graph (own numbering), one array per graph."""
+    def batch_labels_all(self, out=None):
+        """Best labels of every graph (own numbering), one array per graph; out
+        (optional): a uint32 array of at least the batch's vertex count to copy
+        into (pinned memory makes the copy a plain DMA)."""
         G = self.batch_size()
         off = np.zeros(G + 1, np.uint64)
         self._check(lib().scd_batch_labels_all(self._ctx, None, _p(off)))
-        out = np.empty(max(int(off[-1]), 1), np.uint32)
+        if out is None or out.size < int(off[-1]):
+            out = np.empty(max(int(off[-1]), 1), np.uint32)
         self._check(lib().scd_batch_labels_all(self._ctx, _p(out), None))
         return [out[int(off[g]):int(off[g + 1])] for g in range(G)]
 
