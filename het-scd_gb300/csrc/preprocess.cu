@@ -143,8 +143,8 @@ __global__ void k_out_ranges(const uint32_t *__restrict__ indices, const uint32_
 __global__ void k_flag_degrees(const uint32_t *__restrict__ orow, const uint32_t *__restrict__ ocol,
                                const uint8_t *__restrict__ flag, uint32_t count, int32_t *tri_deg) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        if (flag[i]) {
-            atomicAdd(tri_deg + orow[i], 1);
+        if (flag[i]) {   // out-slots are grouped by row: one atomic per row and warp for that side
+            warp_atomic_inc((uint32_t *)(tri_deg + orow[i]), __activemask());
             atomicAdd(tri_deg + ocol[i], 1);
         }
     }
