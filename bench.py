@@ -147,6 +147,34 @@ def cpu_sample_run(threads=None):
     return pairs.shape[0] / (t_ms / 1e3), t_ms, pairs.shape[0], "port"
 
 
+def time_wcc_static(S, eng, gd):
+    """scd_wcc_static (no device allocation) on the resident graph and its current
+    labels: CUDA-event time per call (3 calls after one warm-up) and equality with
+    scd_compute_wcc.  Not part of the step."""
+    import numpy as np
+    import torch
+    lab = eng.current_labels()
+    sizes = eng.community_stats()[0]
+    want = eng.compute_wcc()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a).view(np.int32)).cuda()
+    ind, adj, tri, tdg = dev(gd["indices"]), dev(gd["adj"]), dev(gd["tri"]), dev(gd["tri_deg"])
+    lb, sz = dev(lab), dev(sizes if sizes.size else np.zeros(1, np.int32))
+    out = torch.zeros(1, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    call = lambda: S.lib().scd_wcc_static(ind.data_ptr(), adj.data_ptr(), tri.data_ptr(), tdg.data_ptr(),
+                                          lb.data_ptr(), sz.data_ptr(), int(lab.size), 1.0, out.data_ptr(),
+                                          st.cuda_stream)
+    assert call() == S.OK
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(3):
+        assert call() == S.OK
+    e1.record(st)
+    torch.cuda.synchronize()
+    return {"ms_per_call": e0.elapsed_time(e1) / 3, "equal_to_scd_compute_wcc": float(out.item()) == want,
+            "n": int(lab.size)}
+
+
 def cpu_model():
     """The host CPU's model name (lscpu on Arm, /proc/cpuinfo elsewhere)."""
     try:
@@ -428,7 +456,7 @@ def per_graph_loop(S, device, graphs):
     """The plain per-graph loop: one engine, each graph converted, run to
     convergence and its labels copied out before the next (the reference's one
     graph per main-gpu process, src/main-gpu.cpp:43-110, without process start-up).
-    Returns (seconds, iterations, best WCC, labels) per graph."""
+    Returns the total seconds and (iterations, best WCC, labels, seconds) per graph."""
     import numpy as np
     import torch
     plain = S.Engine(device)
@@ -438,12 +466,13 @@ def per_graph_loop(S, device, graphs):
     out = []
     t = time.perf_counter()
     for p in graphs:
+        t0 = time.perf_counter()
         plain.convert_edges(p)
         if plain.graph_info()[0] == 0:
-            out.append((0, 0.0, np.zeros(0, np.uint32)))
+            out.append((0, 0.0, np.zeros(0, np.uint32), time.perf_counter() - t0))
             continue
         r = plain.run(0.01, 1000)
-        out.append((r["iterations"], r["best_wcc"], plain.labels_from_device()))
+        out.append((r["iterations"], r["best_wcc"], plain.labels_from_device(), time.perf_counter() - t0))
     torch.cuda.synchronize()
     secs = time.perf_counter() - t
     plain.close()
@@ -477,7 +506,7 @@ def bench_served(S, device, args):
     capacity = len(reqs) / (max(h.finished for h in handles) - t)
     cap_cosched = srv.mean_coscheduled()
     same = all(h.result["iterations"] == it and h.result["best_wcc"] == w and np.array_equal(h.labels, lab)
-               for h, (it, w, lab) in zip(handles, loop_out) if it > 0)
+               for h, (it, w, lab, _) in zip(handles, loop_out) if it > 0)
     rate = args.serve_rate if args.serve_rate > 0 else 0.75 * capacity
     rng = np.random.default_rng(55)
     gaps = rng.exponential(1.0 / rate, size=len(reqs))
@@ -498,7 +527,7 @@ def bench_served(S, device, args):
         h.wait(1200)
     end = max(h.finished for h in handles)
     same = same and all(h.result["iterations"] == it and np.array_equal(h.labels, lab)
-                        for h, (it, w, lab) in zip(handles, loop_out) if it > 0)
+                        for h, (it, w, lab, _) in zip(handles, loop_out) if it > 0)
     lanes = [{"max_records": (srv.bounds[k] if k < len(srv.bounds) else None), "steps": len(ln.step_running),
               "mean_coscheduled": float(np.mean(ln.step_running)) if ln.step_running else 0.0,
               **{k2: round(v, 1) if isinstance(v, float) else v for k2, v in ln.set.resident_timing().items()}}
@@ -509,13 +538,21 @@ def bench_served(S, device, args):
     span = end - t
     sizes = [b[0] for b in srv.batches]
     loop_gps = len(reqs) / loop_s
+    # where the loop's time goes: requests of the first lane (<= 2^21 records, the planted
+    # graphs) and the rest (the R-MAT graphs); the large ones are already one graph per
+    # launch-filling pipeline, so co-scheduling cannot take the loop below their share
+    big = [x[3] for p, x in zip(reqs, loop_out) if p.shape[0] > (1 << 21)]
+    small = [x[3] for p, x in zip(reqs, loop_out) if p.shape[0] <= (1 << 21)]
     return {"workload": "Poisson arrivals; 80% planted n log-uniform [1000,50000] degree 16 mu 0.1, "
                         "20% R-MAT scale 19-21 edge factor 16",
             "requests": len(reqs), "capacity_graphs_per_s": capacity, "offered_per_s": rate,
             "graphs_per_s": len(reqs) / span,
             "edges_per_s": sum(p.shape[0] for p in reqs) / span,
             "p50_ms": serve.percentile(lat, 50), "p99_ms": serve.percentile(lat, 99), "max_ms": max(lat),
-            "per_graph_loop": {"graphs_per_s": loop_gps, "seconds": loop_s},
+            "per_graph_loop": {"graphs_per_s": loop_gps, "seconds": loop_s,
+                               "seconds_requests_le_2e21_records": round(sum(small), 4), "count_small": len(small),
+                               "seconds_requests_gt_2e21_records": round(sum(big), 4), "count_large": len(big),
+                               "speedup_bound_if_small_ones_were_free": loop_s / max(sum(big), 1e-9)},
             "speedup_vs_loop": capacity / loop_gps, "identical_to_loop": bool(same),
             "mean_coscheduled_graphs": {"capacity_run": cap_cosched, "poisson_run": srv.mean_coscheduled()},
             "converters": args.serve_converters, "budget_gb": 120, "peak_admitted_gb": srv.peak_in_use / 1e9,
@@ -724,6 +761,7 @@ def bench_plain(S, args, world, rank, local, dist):
             "stages": stages,
             "clocks": ck, "generate_s": round(gen_s, 2)}
     best_labels = eng.labels_from_device()
+    line["wcc_static"] = time_wcc_static(S, eng, gd)
     eng.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
