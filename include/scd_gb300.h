@@ -305,12 +305,15 @@ int scd_resident_timing(scd_ctx *set, double *ms_steps, double *ms_rebuild, doub
  * cudaStream_t, NULL for the default stream) of the current device and the
  * call returns without waiting.  The value equals scd_compute_wcc's for the
  * same graph and labels.
- * Scratch: a fixed array of SCD_WCC_STATIC_MAX_VERTICES/2048 doubles (64 KB)
- * inside the library, allocated when the library is loaded and held by every
- * GPU that uses it until the process exits; n above SCD_WCC_STATIC_MAX_VERTICES
- * returns SCD_ERR_LIMIT.  All calls share that array: calls that may overlap
- * on the GPU (different streams without ordering) race and must be ordered by
- * the caller.  The first call on a device looks up the array's device address
+ * Scratch: two fixed arrays inside the library, allocated when the library is
+ * loaded and held by every GPU that uses it until the process exits: the block
+ * partials of the sum (SCD_WCC_STATIC_MAX_VERTICES/2048 doubles, 64 KB) and the
+ * internal-triangle counts of hub rows (the first 131072 vertices of degree > 128,
+ * 1 MB; convert's ids are degree ranks, so those are its hubs; a hub beyond them
+ * takes a slower path to the same value).  n above SCD_WCC_STATIC_MAX_VERTICES
+ * returns SCD_ERR_LIMIT.  All calls share the arrays: calls that may overlap on
+ * the GPU (different streams without ordering) race and must be ordered by the
+ * caller.  The first call on a device looks up the array's device address
  * and must come before any stream capture (a first call made while its stream
  * is being captured returns SCD_ERR_STATE).  Every later call made outside a
  * capture looks the address up again, so a device reset or a new primary

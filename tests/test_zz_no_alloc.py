@@ -99,6 +99,50 @@ def test_static_wcc_skip_branches_match_engine():
     assert got == want, (got, want)
 
 
+def test_static_wcc_hubs_at_high_ids_match_engine():
+    """Hub rows at ids beyond the first 131072 vertices (whose hub counts the
+    library spreads over many CTAs) take the one-warp-per-vertex path: an R-MAT
+    graph renumbered in reverse behind 100,000 isolated vertices puts its hubs
+    there; the value still equals scd_compute_wcc's bit for bit."""
+    torch = pytest.importorskip("torch")
+    import oracle as O
+    import scdgen
+    lib = S.lib()
+    with S.Engine(0) as eng:
+        eng.convert_edges(scdgen.rmat(17, 16, seed=23))
+        g = eng.graph_download()
+    n0, pad = g["n"], 100000
+    n = n0 + pad
+    deg = np.diff(g["indices"].astype(np.int64))
+    new_of = (n - 1 - np.arange(n0)).astype(np.uint32)          # old id v -> n-1-v: hubs last
+    old_of = np.full(n, 0xFFFFFFFF, np.uint32)
+    old_of[new_of] = np.arange(n0, dtype=np.uint32)
+    ndeg = np.zeros(n, np.int64)
+    ndeg[new_of] = deg
+    ind = np.zeros(n + 1, np.uint32)
+    ind[1:] = np.cumsum(ndeg)
+    adj = np.empty_like(g["adj"])
+    for v in range(n0):
+        row = new_of[g["adj"][g["indices"][v]:g["indices"][v + 1]]]
+        w = new_of[v]
+        adj[ind[w]:ind[w + 1]] = np.sort(row)
+    tri = np.zeros(n, np.int32)
+    tdg = np.zeros(n, np.int32)
+    tri[new_of] = g["tri"]
+    tdg[new_of] = g["tri_deg"]
+    assert int(new_of[0]) >= 131072 and deg[0] > 128            # the biggest hub lies beyond the hub slots
+    graph = dict(n=n, m=g["m"], indices=ind, adj=adj, tri=tri, tri_deg=tdg)
+    lab = np.full(n, S.INVALID_LABEL, np.uint32)
+    lab[new_of] = (np.arange(n0) * 2654435761 % (n0 // 12)).astype(np.uint32)   # communities of ~12
+    with S.Engine(0) as eng:
+        eng.transfer_graph(O.Graph(n, g["m"], ind, adj, tri, tdg))
+        eng.labels_to_device(lab)
+        want = eng.compute_wcc()
+        sizes = eng.community_stats()[0].copy()
+    got = _static_wcc(lib, torch, graph, lab, sizes)
+    assert got == want, (got, want)
+
+
 def test_static_wcc_limits_and_arguments():
     lib = S.lib()
     dummy = ctypes.c_void_p(1)
