@@ -458,26 +458,36 @@ void collect_stats(Ctx &c, const uint32_t *labels, Stats &st, bool frozen_graphs
 // unlabelled vertices and those of converged graphs.  The internal triangles of
 // compute_wcc (src/wcc.cpp:84-127) are exactly the triangles of this subgraph, so
 // the count walks internal lists only instead of filtering whole out-lists.
+template <int G>
 __global__ void __launch_bounds__(TPB)
 k_internal_outlists(uint32_t n, const uint32_t *__restrict__ indices, const uint32_t *__restrict__ nlow,
                     const uint32_t *__restrict__ adj, LabelFilter lf, uint32_t *ilen, uint32_t *iadj) {
-    const int lane = threadIdx.x & 31;
+    // a group of G lanes per vertex (out-lists of most vertices are short; ids are
+    // degree ranks, so the vertices of a warp have out-lists of similar length)
+    const int lane = threadIdx.x & 31, gl = lane % G, g0 = lane - gl;
+    const unsigned gmask = (G == 32) ? FULL : (((1u << G) - 1u) << g0);
     const unsigned lt = (1u << lane) - 1u;
-    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += (gridDim.x * blockDim.x) >> 5) {
-        const uint32_t l = lf.labels[v];
+    const uint32_t groups = (gridDim.x * blockDim.x) / G;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) / G - (lane / G); base < n;
+         base += groups) {
+        const uint32_t v = base + lane / G;   // (base: the warp's first vertex)
+        const bool live = v < n;
+        const uint32_t l = live ? lf.labels[v] : INVALID;
+        const bool on = live && l != INVALID && !lf.frozen(v);
+        const uint32_t beg = on ? indices[v] : 0u, len = on ? nlow[v] : 0u;
+        uint32_t steps = (len + G - 1) / G;
+#pragma unroll
+        for (int d = G; d < 32; d <<= 1) steps = max(steps, __shfl_xor_sync(FULL, steps, d));
         uint32_t cnt = 0;
-        if (l != INVALID && !lf.frozen(v)) {
-            const uint32_t beg = indices[v], len = nlow[v];
-            for (uint32_t i0 = 0; i0 < len; i0 += 32) {
-                const uint32_t i = i0 + lane;
-                const uint32_t w = i < len ? adj[beg + i] : 0u;
-                const bool keep = i < len && lf.labels[w] == l;
-                const unsigned kb = __ballot_sync(FULL, keep);
-                if (keep) iadj[beg + cnt + __popc(kb & lt)] = w;
-                cnt += __popc(kb);
-            }
+        for (uint32_t s = 0; s < steps; s++) {
+            const uint32_t i = s * G + gl;
+            const uint32_t w = i < len ? adj[beg + i] : 0u;
+            const bool keep = i < len && lf.labels[w] == l;
+            const unsigned kb = __ballot_sync(FULL, keep) & gmask;
+            if (keep) iadj[beg + cnt + __popc(kb & lt)] = w;
+            cnt += __popc(kb);
         }
-        if (lane == 0) ilen[v] = cnt;
+        if (live && gl == 0) ilen[v] = cnt;
     }
 }
 
@@ -495,7 +505,7 @@ void launch_wcc(Ctx &c, const uint32_t *labels, const Stats &st, bool frozen_gra
     const Batch &b = c.b;
     const uint8_t *active = frozen_graphs ? b.active : nullptr;
     const LabelFilter lf{labels, b.gid, active};
-    k_internal_outlists<<<grid_for((uint64_t)g.n * 32, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj, lf, c.int_len,
+    k_internal_outlists<8><<<grid_for((uint64_t)g.n * 8, TPB), TPB, 0, s>>>(g.n, g.indices, g.nlow, g.adj, lf, c.int_len,
                                                                         c.int_adj);
     CK_LAUNCH("k_internal_outlists");
     // the plan's buckets (by full out-degree) stay valid: internal lists are never longer
