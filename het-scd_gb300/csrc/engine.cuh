@@ -131,7 +131,7 @@ struct LabelFilter {
 // buckets, then the in-list centres: a vertex b whose edges a -> b with
 // d+(a) < d+(b) (b-centric edges, below) are counted from b's table.
 struct TcPlan {
-    static constexpr int K = 6;
+    static constexpr int K = 7;
     uint32_t *verts[K] = {};
     uint32_t *unit_off[K] = {};
     uint32_t nverts[K] = {};

@@ -566,9 +566,9 @@ constexpr uint32_t B2 = 8192;
 }  // namespace
 
 void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists) {
-    const uint32_t sm = c.tc_small, s16 = sm < 16 ? sm : 16, b0 = c.tc_b0 > sm ? c.tc_b0 : sm;
-    const uint32_t bounds[TcPlan::K + 1] = {0, s16, sm, b0, c.tc_b1, B2, 0xffffffffu};
-    const uint32_t per_unit[TcPlan::K] = {1, 1, 32, CTA1_THREADS * CTA1_ROUNDS, CTA2_THREADS * CTA2_ROUNDS, 1};
+    const uint32_t sm = c.tc_small, s16 = sm < 16 ? sm : 16, s8 = sm < 8 ? sm : 8, b0 = c.tc_b0 > sm ? c.tc_b0 : sm;
+    const uint32_t bounds[TcPlan::K + 1] = {0, s8, s16, sm, b0, c.tc_b1, B2, 0xffffffffu};
+    const uint32_t per_unit[TcPlan::K] = {1, 1, 1, 32, CTA1_THREADS * CTA1_ROUNDS, CTA2_THREADS * CTA2_ROUNDS, 1};
     const bool split = in_lists && !(c.flags & SCD_FLAG_TC_OUT_ONLY);
     plan.dir_lo = split ? b0 : 0;
     plan.dir_hi = split ? B2 : 0;
@@ -576,7 +576,7 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
     // every bucket's scans first, then one host read of all the counts
     DevBuf<uint32_t> pos[TcPlan::K], ipos[TcPlan::K], counts(2 * TcPlan::K, s);
     for (int k = 0; k < TcPlan::K; k++) {
-        const bool cta = k == 3 || k == 4;
+        const bool cta = k == 4 || k == 5;
         pos[k].alloc((size_t)o.n + 1, s);
         scan_exclusive<uint32_t>(InBucket{o, bounds[k], bounds[k + 1], false}, pos[k].get(), o.n, s);
         CK(cudaMemcpyAsync(counts.get() + 2 * k, pos[k].get() + o.n, 4, cudaMemcpyDeviceToDevice, s));
@@ -707,34 +707,40 @@ void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter 
     CK(cudaMemsetAsync(ctr, 0, 16, s));
     const Dir dir{plan.dir_lo, plan.dir_hi, plan.dir_amin};
     if (plan.nverts[0]) {
-        k_tc_small<16><<<grid_for((uint64_t)plan.nverts[0] * 16, 256, 152 * 8), 256, 0, s>>>(
+        k_tc_small<8><<<grid_for((uint64_t)plan.nverts[0] * 8, 256, 152 * 8), 256, 0, s>>>(
             o, plan.verts[0], plan.nverts[0], dir, labels, tcount, flag);
-        CK_LAUNCH("k_tc_small16");
+        CK_LAUNCH("k_tc_small8");
         c.launches++;
     }
     if (plan.nverts[1]) {
-        k_tc_small<32><<<grid_for((uint64_t)plan.nverts[1] * 32, 256, 152 * 8), 256, 0, s>>>(
+        k_tc_small<16><<<grid_for((uint64_t)plan.nverts[1] * 16, 256, 152 * 8), 256, 0, s>>>(
             o, plan.verts[1], plan.nverts[1], dir, labels, tcount, flag);
-        CK_LAUNCH("k_tc_small32");
+        CK_LAUNCH("k_tc_small16");
         c.launches++;
     }
     if (plan.nverts[2]) {
-        k_tc_warp<16, 256, 64, 10><<<152 * 4, 16 * 32, 0, s>>>(o, plan.verts[2], plan.unit_off[2], plan.nverts[2],
+        k_tc_small<32><<<grid_for((uint64_t)plan.nverts[2] * 32, 256, 152 * 8), 256, 0, s>>>(
+            o, plan.verts[2], plan.nverts[2], dir, labels, tcount, flag);
+        CK_LAUNCH("k_tc_small32");
+        c.launches++;
+    }
+    if (plan.nverts[3]) {
+        k_tc_warp<16, 256, 64, 10><<<152 * 4, 16 * 32, 0, s>>>(o, plan.verts[3], plan.unit_off[3], plan.nverts[3],
                                                            dir, labels, tcount, flag, ctr);
         CK_LAUNCH("k_tc_warp64");
         c.launches++;
     }
-    if (plan.nverts[3]) {
-        launch_tc_cta<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14, 12>(o, plan, 3, labels, tcount, flag, ctr + 1, 152 * 12,
+    if (plan.nverts[4]) {
+        launch_tc_cta<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14, 12>(o, plan, 4, labels, tcount, flag, ctr + 1, 152 * 12,
                                                                      s);
         c.launches++;
     }
-    if (plan.nverts[4]) {
-        launch_tc_cta<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17, 1>(o, plan, 4, labels, tcount, flag, ctr + 2, 152, s);
+    if (plan.nverts[5]) {
+        launch_tc_cta<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17, 1>(o, plan, 5, labels, tcount, flag, ctr + 2, 152, s);
         c.launches++;
     }
-    if (plan.nverts[5]) {
-        k_tc_huge<<<152 * 4, 256, 0, s>>>(o, plan.verts[5], plan.nverts[5], labels, tcount, flag);
+    if (plan.nverts[6]) {
+        k_tc_huge<<<152 * 4, 256, 0, s>>>(o, plan.verts[6], plan.nverts[6], labels, tcount, flag);
         CK_LAUNCH("k_tc_huge");
         c.launches++;
     }
