@@ -115,6 +115,23 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(dist, values, device):
+    """Each value's maximum over all ranks (replicas: the slowest one sets the job's
+    time); the values unchanged on one process (dist None)."""
+    if not dist:
+        return list(values)
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def job_throughput(world, units_per_replica, ms):
+    """Whole-job rate of N independent replicas timed together: all the units over
+    the slowest replica's time."""
+    return world * units_per_replica / (ms / 1e3)
+
+
 def measured_peak_gbs():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -706,10 +723,7 @@ def bench_plain(S, args, world, rank, local, dist):
     torch.cuda.synchronize()
     text_ms = (time.perf_counter() - t) * 1e3 / args.steps
 
-    if dist:
-        tt = torch.tensor([dev_ms, e2e_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_ms, e2e_ms = tt.tolist()
+    dev_ms, e2e_ms = max_over_ranks(dist, [dev_ms, e2e_ms], "cuda")
 
     # roofline of the dominant kernel: preprocessing triangle counting
     gd = eng.graph_download()
@@ -741,13 +755,13 @@ def bench_plain(S, args, world, rank, local, dist):
     for v in stages.values():
         v["frac"] = v["gbs"] / peak
 
-    line = {"metric": METRIC, "value": world * E / (dev_ms / 1e3), "unit": UNIT, "n_gpus": world,
+    line = {"metric": METRIC, "value": job_throughput(world, E, dev_ms), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64", "data": "synthetic",
             "config": {"workload": f"rmat-{args.scale}", "edge_factor": 16, "abcd": [0.57, 0.19, 0.19, 0.05],
                        "edges_in": E, "n": n, "m": m, "iterations": r["iterations"], "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (edge list %d MB)" % (E * 8 >> 20)},
-            "e2e": {"value": world * E / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": E * 8,
+            "e2e": {"value": job_throughput(world, E, e2e_ms), "unit": UNIT, "h2d_bytes_per_step": E * 8,
                     "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1)},
             "e2e_text": {"value": world * E / (text_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": len(text),
                          "d2h_bytes_per_step": n * 4 + 8 * (r2["iterations"] + 1),
