@@ -115,6 +115,8 @@ def test_many_graphs_joining_from_another_thread_equal_alone():
                 out[gid] = (res, lab)
         t.join()
         info = rs.resident_info()
+        rs.resident_step()                         # every graph taken: the union is dropped
+        assert rs.resident_info()["graphs"] == 0 and rs.memory_usage() == 0
     assert len(out) == len(graphs)
     for gid, (res, lab) in out.items():
         _check(graphs[ids[gid]], res, lab)
