@@ -139,10 +139,32 @@ struct TcPlan {
     uint32_t dir_lo = 0, dir_hi = 0, dir_amin = 0;   // b-centric iff d+(a) < d+(b),
                                                       // dir_lo < d+(b) <= dir_hi, d+(a) > dir_amin
     DevBuf<uint32_t> tmp[2 * K];   // storage when the plan is temporary
+    // Core map of the upper CTA bucket (tc_core_map): the vertices of degree >
+    // cta_hi, numbered 0..core_n-1 in id order.  core_adj holds every out-list
+    // in core numbers (core_n for a vertex outside the core), v's list at
+    // core_adj[core_beg[v]..], each list starting on a 16-byte boundary and
+    // padded with core_n to a multiple of 4 entries.  Every out-list of a centre
+    // of that bucket lies in the core, so a bitmap of core_n bits holds it
+    // exactly.  core_n == 0: no map (the hash-table kernels run); core_lcap:
+    // the bucket's largest out-degree (rounded up to even).
+    const uint32_t *core_adj = nullptr, *core_beg = nullptr;
+    uint32_t core_n = 0, core_lcap = 0;
+    uint32_t cta_lo = 0, cta_hi = 0;   // out-degree range (cta_lo, cta_hi] of the first CTA bucket
+    DevBuf<uint32_t> core_buf, core_beg_buf;
 };
 struct Ctx;
 // in_lists: also in-list centres (b-centric edges) in the CTA buckets
-void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists);
+// core_split: the upper CTA bucket starts at tc_core (the core-bitmap kernel's
+// split, for a plan that gets a core map) instead of tc_b1
+void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists,
+             bool core_split = false);
+// builds the core map of the upper CTA bucket for out-lists o.adj[0..slots)
+// (symmetric degree of v = o.len[v] + o.in_len(v)); leaves core_n = 0 when the
+// core's bitmap would not fit the core kernel's shared memory
+void tc_core_map(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s);
+// the plan of a full count (preprocessing) over out-lists o.adj[0..slots) with in-list
+// centres: the core split and its core map, or the hash kernels' split
+void tc_plan_counting(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s);
 // tcount[v] += triangles at v; flag[slot] = 1 for out-slots on a triangle.
 // With labels: internal triangles only.  tcount and flag must be zeroed.
 // Sorts every row of a CSR (offsets off[nrows+1], values vals) ascending in place;
@@ -180,6 +202,7 @@ struct Ctx {
     std::string err;
     uint64_t launches = 0;
     uint32_t tc_small = 32, tc_b0 = 64, tc_b1 = 1024;   // triangle-counting bucket splits (autotuned)
+    uint32_t tc_core = 256;   // preprocessing count: out-degree from which the core-bitmap kernel runs
     uint32_t tc_amin = 0;   // b-centric edges need d+(a) > tc_amin (autotuned; at most tc_small)
 
     Graph g;

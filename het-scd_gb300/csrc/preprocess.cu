@@ -454,7 +454,7 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     Oriented o{obeg.get(), olen.get(), ocol.get(), n1, ibeg.get(), ilen.get(), icol.get()};
     {
         TcPlan plan;
-        tc_plan(c, o, plan, s, false, true);
+        tc_plan_counting(c, o, m1, plan, s);
         count_triangles(c, o, plan, LabelFilter{}, tcount.get(), oflag.get(), s);
     }
     icol.release();

@@ -36,6 +36,11 @@
 // (coalesced loads), walking the partner boundaries forward.  Centres are
 // grouped by out-degree into buckets so that each kernel's shared memory
 // matches its lists.
+//
+// The preprocessing count takes its upper CTA bucket (out-degree > 256, where
+// nearly all the work of skewed graphs lies) with an exact bitmap instead of a
+// hash table: those centres' out-lists all lie among the vertices of degree >
+// 256, numbered densely, so a small shared bitmap holds each one (k_tc_core).
 #include "engine.cuh"
 
 namespace scd {
@@ -518,6 +523,197 @@ void launch_tc_cta(const Oriented &o, const TcPlan &plan, int k, LabelFilter lab
 // partners per CTA unit of the two CTA buckets
 constexpr int CTA1_THREADS = 128, CTA1_ROUNDS = 4, CTA2_THREADS = 256, CTA2_ROUNDS = 2;
 
+// CTA units of the upper CTA bucket (out-degree in (cta_hi, 8192]) over a core
+// bitmap, when the plan has a core map and no labels filter.  Every out-list
+// of such a centre lies in the core, the vertices of degree > cta_hi (their
+// degrees are at least the centre's), so the centre's out-list in core numbers
+// is held exactly by a shared bitmap of core_n bits (plus the outside marker
+// core_n, never set).  pre[w] is the out-list position of the first member in
+// bitmap word w; core numbers ascend with ids, so the position of a member c
+// is pre[c/32] + the popcount of the word's bits below c.  A lookup is one
+// shared load and a bit test: no hash, no probe sequence, no false positives.
+// The core of the upper bucket is small (R-MAT scale 22: 110,035 vertices of
+// degree > 256, a 13 KB bitmap), so many CTAs share an SM.
+//
+// The walk: THREADS partners per round; every list in the core-number array
+// starts on a 16-byte boundary and is padded with core_n to whole quads, the
+// quads of the round are flattened by a block scan, and a warp takes 32 x K
+// consecutive quads, lane L every 32nd (one 16-byte load each: 4K items of a
+// lane in flight).  A hit flags the walked slot at once and counts in the
+// member's 16-bit shared count and, per quad, in the partner's shared count.
+template <int THREADS, int K>
+__global__ void __launch_bounds__(THREADS)
+k_tc_core(Oriented o, const uint32_t *__restrict__ cpad, const uint32_t *__restrict__ cbeg, uint32_t core_n,
+          uint32_t kwords, uint32_t lcap, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off,
+          uint32_t nverts, uint32_t nfwd, uint32_t per_unit, Dir dir, uint32_t *tcount, uint8_t *flag,
+          uint32_t *next_unit) {
+    extern __shared__ __align__(16) uint32_t sm[];
+    uint32_t *bm = sm;                                    // kwords
+    uint32_t *cnt = bm + kwords;                          // lcap 16-bit counts
+    uint16_t *pre = (uint16_t *)(cnt + (lcap + 1) / 2);   // kwords
+    __shared__ uint32_t qpre[THREADS], sq0[THREADS], sdl[THREADS], sh[THREADS], wsum[THREADS / 32];
+    __shared__ uint32_t s_unit, s_total, s_xhits;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint4 *cq = reinterpret_cast<const uint4 *>(cpad);
+    for (uint32_t i = threadIdx.x; i < kwords; i += THREADS) bm[i] = 0;
+    const uint32_t n_units = unit_off[nverts];
+    while (true) {
+        if (threadIdx.x == 0) {
+            s_unit = atomicAdd(next_unit, 1u);
+            s_xhits = 0;
+        }
+        __syncthreads();
+        const uint32_t unit = s_unit;
+        if (unit >= n_units) break;
+        uint32_t lo = 0, hi = nverts + 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (unit_off[mid] <= unit) lo = mid + 1;
+            else hi = mid;
+        }
+        const uint32_t vi = lo - 1;
+        const uint32_t x = verts[vi], ch = unit - unit_off[vi];
+        const bool fwd = vi < nfwd;
+        const uint32_t xbeg = o.beg[x], xlen = o.len[x];
+        const uint32_t *xc = cpad + cbeg[x];
+        for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) {
+            const uint32_t c = xc[i];
+            if (c < core_n) {
+                atomicOr(&bm[c >> 5], 1u << (c & 31));
+                if (i == 0 || (xc[i - 1] >> 5) != (c >> 5)) pre[c >> 5] = (uint16_t)i;
+            }
+        }
+        for (uint32_t i = threadIdx.x; i < (xlen + 1) / 2; i += THREADS) cnt[i] = 0;
+        const uint32_t *padj = fwd ? o.adj : o.in_adj();
+        const uint32_t pbeg = fwd ? xbeg : o.in_beg(x), plen = fwd ? xlen : o.in_len(x);
+        const uint32_t pend = min(plen, (ch + 1) * per_unit);
+        uint32_t xh = 0;
+        for (uint32_t r0 = ch * per_unit; r0 < pend; r0 += THREADS) {
+            const uint32_t j = r0 + threadIdx.x;
+            uint32_t y = 0, wb = 0, cb = 0, ob = 0;
+            if (j < pend) {
+                y = padj[pbeg + j];
+                const uint32_t dy = o.len[y];
+                if (fwd ? !dir.bcentric(xlen, dy) : dir.bcentric(dy, xlen)) {
+                    wb = dy;
+                    cb = cbeg[y];
+                    ob = o.beg[y];
+                }
+            }
+            const uint32_t nq = (wb + 3) >> 2;
+            uint32_t incl = warp_inclusive_scan(nq);   // block scan of the quad counts
+            if (lane == 31) wsum[w] = incl;
+            __syncthreads();   // also orders the bitmap build before the walk
+            if (threadIdx.x == 0) {
+                uint32_t run = 0;
+                for (int k = 0; k < THREADS / 32; k++) {
+                    const uint32_t v = wsum[k];
+                    wsum[k] = run;
+                    run += v;
+                }
+                s_total = run;
+            }
+            __syncthreads();
+            qpre[threadIdx.x] = incl + wsum[w] - nq;
+            sq0[threadIdx.x] = cb >> 2;
+            sdl[threadIdx.x] = ob - cb;   // core-array position -> out-slot (mod 2^32)
+            sh[threadIdx.x] = 0;
+            const uint32_t total = s_total;
+            __syncthreads();
+            for (uint32_t t0 = (uint32_t)w * 32 * K; t0 < total; t0 += THREADS * K) {
+                const uint32_t tl = t0 + lane;
+                uint32_t l0 = 0, l1 = THREADS;   // owner of tl: last partner with qpre <= tl
+                while (l0 < l1) {
+                    const uint32_t mid = (l0 + l1) >> 1;
+                    if (qpre[mid] <= tl) l0 = mid + 1;
+                    else l1 = mid;
+                }
+                uint32_t jb = l0 - 1;
+                uint32_t nxt = jb + 1 < THREADS ? qpre[jb + 1] : total;
+                uint4 v[K];
+                uint32_t qa[K], own[K];
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    const uint32_t t = tl + 32 * k;
+                    own[k] = INVALID;
+                    if (t < total) {
+                        while (t >= nxt) {
+                            jb++;
+                            nxt = jb + 1 < THREADS ? qpre[jb + 1] : total;
+                        }
+                        own[k] = jb;
+                        qa[k] = sq0[jb] + (t - qpre[jb]);
+                        v[k] = __ldg(cq + qa[k]);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < K; k++) {
+                    if (own[k] == INVALID) continue;
+                    const uint32_t fo = qa[k] * 4 + sdl[own[k]];
+                    const uint32_t vals[4] = {v[k].x, v[k].y, v[k].z, v[k].w};
+                    uint32_t h = 0;
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const uint32_t c = vals[e], wd = bm[c >> 5], bit = c & 31;
+                        if ((wd >> bit) & 1u) {
+                            const uint32_t r = pre[c >> 5] + __popc(wd & ((1u << bit) - 1u));
+                            if (r < xlen) atomicAdd(&cnt[r >> 1], 1u << ((r & 1) << 4));
+                            flag[fo + e] = 1;
+                            h++;
+                        }
+                    }
+                    if (h) atomicAdd(&sh[own[k]], h);
+                }
+            }
+            __syncthreads();
+            const uint32_t hb = j < pend ? sh[threadIdx.x] : 0u;
+            if (hb) {
+                atomicAdd(tcount + y, hb);
+                flag[fwd ? xbeg + j : ob + lower_bound(o.adj + ob, wb, x)] = 1;
+                xh += hb;
+            }
+        }
+        xh = warp_sum(xh);
+        if (lane == 0 && xh) atomicAdd(&s_xhits, xh);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_xhits) atomicAdd(tcount + x, s_xhits);
+        const uint32_t *xa = o.adj + xbeg;
+        for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) {
+            const uint32_t cc = (cnt[i >> 1] >> ((i & 1) << 4)) & 0xffffu;
+            if (cc) {
+                atomicAdd(tcount + xa[i], cc);
+                flag[xbeg + i] = 1;
+            }
+            const uint32_t c = xc[i];
+            if (c < core_n) bm[c >> 5] = 0;
+        }
+        __syncthreads();
+    }
+}
+
+constexpr int CORE_THREADS = 256, CORE_K = 2;
+constexpr size_t CORE_SMEM_MAX = 200 * 1024;   // below the 227 KB opt-in limit with the static part
+
+inline size_t tc_core_smem(uint32_t kwords, uint32_t lcap) {
+    return (size_t)kwords * 4 + (size_t)(lcap + 1) / 2 * 4 + ((size_t)kwords * 2 + 3) / 4 * 4;
+}
+
+void launch_tc_core(const Oriented &o, const TcPlan &plan, int k, uint32_t lcap, uint32_t *tcount, uint8_t *flag,
+                    uint32_t *ctr, cudaStream_t s) {
+    const uint32_t kwords = plan.core_n / 32 + 1;
+    const size_t smem = tc_core_smem(kwords, lcap);
+    const void *fn = (const void *)k_tc_core<CORE_THREADS, CORE_K>;
+    int dev = 0, per_sm = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CORE_THREADS, smem));
+    if (per_sm < 1) throw Error(SCD_ERR_CUDA, "core triangle-count kernel does not fit an SM");
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    k_tc_core<CORE_THREADS, CORE_K><<<sms * per_sm, CORE_THREADS, smem, s>>>(
+        o, plan.core_adj, plan.core_beg, plan.core_n, kwords, lcap, plan.verts[k], plan.unit_off[k], plan.nverts[k],
+        plan.nfwd[k], CTA2_THREADS * CTA2_ROUNDS, Dir{plan.dir_lo, plan.dir_hi, plan.dir_amin}, tcount, flag, ctr);
+    CK_LAUNCH("k_tc_core");
+}
+
 // Lists longer than 8192 (none in the benchmark graphs): items looked up
 // by binary search in the sorted out-list in global memory, per-triangle
 // atomics.  Kept for generality.
@@ -563,16 +759,62 @@ k_tc_huge(Oriented o, const uint32_t *__restrict__ verts, uint32_t nverts, Label
 // (the kernels' shared-memory capacities); S, B0, B1 tuned per context
 constexpr uint32_t B2 = 8192;
 
+
+// v lies in the core: symmetric degree above the CTA buckets' lower bound
+struct CoreFlag {
+    Oriented o;
+    uint32_t bound;
+    __device__ uint32_t operator[](size_t v) const { return o.len[v] + o.in_len((uint32_t)v) > bound; }
+};
+
+// largest out-degree among the centres verts[0..n)
+__global__ void k_max_len(const uint32_t *__restrict__ len, const uint32_t *__restrict__ verts, uint32_t n,
+                          uint32_t *mx) {
+    uint32_t m = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, len[verts[i]]);
+    for (int d = 16; d > 0; d >>= 1) m = max(m, __shfl_xor_sync(FULL, m, d));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(mx, m);
+}
+
+// padded list length: every list starts on a 16-byte boundary
+struct PadLen {
+    const uint32_t *len;
+    __device__ uint32_t operator[](size_t v) const { return (len[v] + 3u) & ~3u; }
+};
+
+// v's out-list in core numbers (core_n: outside the core) at cpad[cbeg[v]..],
+// padded with core_n to a multiple of 4; one warp per vertex
+__global__ void k_core_pad(Oriented o, const uint32_t *__restrict__ cpos, uint32_t core_n,
+                           const uint32_t *__restrict__ cbeg, uint32_t *cpad) {
+    const uint32_t lane = threadIdx.x & 31, warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < o.n; v += warps) {
+        const uint32_t len = o.len[v], b = o.beg[v], d = cbeg[v], plen = (len + 3u) & ~3u;
+        for (uint32_t i = lane; i < plen; i += 32) {
+            uint32_t c = core_n;
+            if (i < len) {
+                const uint32_t u = o.adj[b + i], a = cpos[u];
+                if (cpos[u + 1] > a) c = a;
+            }
+            cpad[d + i] = c;
+        }
+    }
+}
+
 }  // namespace
 
-void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists) {
+void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists, bool core_split) {
     const uint32_t sm = c.tc_small, s16 = sm < 16 ? sm : 16, s8 = sm < 8 ? sm : 8, b0 = c.tc_b0 > sm ? c.tc_b0 : sm;
-    const uint32_t bounds[TcPlan::K + 1] = {0, s8, s16, sm, b0, c.tc_b1, B2, 0xffffffffu};
+    // the core-bitmap kernel takes the upper CTA bucket from tc_core on; the hash
+    // kernels' upper bucket (one CTA per SM, 16K-entry tables) from tc_b1 on
+    const uint32_t b1 = core_split ? (c.tc_core > b0 ? c.tc_core : b0) : c.tc_b1;
+    const uint32_t bounds[TcPlan::K + 1] = {0, s8, s16, sm, b0, b1, B2, 0xffffffffu};
     const uint32_t per_unit[TcPlan::K] = {1, 1, 1, 32, CTA1_THREADS * CTA1_ROUNDS, CTA2_THREADS * CTA2_ROUNDS, 1};
     const bool split = in_lists && !(c.flags & SCD_FLAG_TC_OUT_ONLY);
     plan.dir_lo = split ? b0 : 0;
     plan.dir_hi = split ? B2 : 0;
     plan.dir_amin = c.tc_amin < sm ? c.tc_amin : sm;
+    plan.cta_lo = b0;
+    plan.cta_hi = b1;
     // every bucket's scans first, then one host read of all the counts
     DevBuf<uint32_t> pos[TcPlan::K], ipos[TcPlan::K], counts(2 * TcPlan::K, s);
     for (int k = 0; k < TcPlan::K; k++) {
@@ -617,6 +859,50 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
     }
 }
 
+void tc_core_map(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s) {
+    plan.core_adj = plan.core_beg = nullptr;
+    plan.core_n = plan.core_lcap = 0;
+    if (o.n == 0 || plan.nverts[5] == 0) return;
+    if (slots + 3ull * o.n >= 0xffffffffull) return;   // the padded layout is indexed in 32 bits
+    DevBuf<uint32_t> cpos((size_t)o.n + 1, s), mx(1, s);
+    plan.core_beg_buf.alloc((size_t)o.n + 1, s);
+    scan_exclusive<uint32_t>(CoreFlag{o, plan.cta_hi}, cpos.get(), o.n, s);
+    scan_exclusive<uint32_t>(PadLen{o.len}, plan.core_beg_buf.get(), o.n, s);
+    CK(cudaMemsetAsync(mx.get(), 0, 4, s));
+    k_max_len<<<grid_for(plan.nverts[5], 256, 152 * 4), 256, 0, s>>>(o.len, plan.verts[5], plan.nverts[5], mx.get());
+    CK_LAUNCH("k_max_len");
+    uint32_t h[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(&h[0], cpos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&h[1], plan.core_beg_buf.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&h[2], mx.get(), 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const uint32_t core_n = h[0], padded = h[1], lcap = (h[2] + 1) & ~1u;
+    if (tc_core_smem(core_n / 32 + 1, lcap) > CORE_SMEM_MAX) {
+        plan.core_beg_buf.release();
+        return;
+    }
+    plan.core_buf.alloc((size_t)padded + 4, s);
+    k_core_pad<<<grid_for((uint64_t)o.n * 32, 256, 152 * 16), 256, 0, s>>>(o, cpos.get(), core_n,
+                                                                           plan.core_beg_buf.get(), plan.core_buf.get());
+    CK_LAUNCH("k_core_pad");
+    c.launches += 2;
+    plan.core_adj = plan.core_buf.get();
+    plan.core_beg = plan.core_beg_buf.get();
+    plan.core_n = core_n;
+    plan.core_lcap = lcap;
+}
+
+void tc_plan_counting(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s) {
+    const bool core = !(c.flags & SCD_FLAG_TC_HASH);
+    tc_plan(c, o, plan, s, false, true, core);
+    if (!core) return;
+    tc_core_map(c, o, slots, plan, s);
+    if (plan.core_n == 0 && plan.nverts[5] && plan.cta_hi != c.tc_b1) {   // no map: the hash kernels' split
+        plan = TcPlan();
+        tc_plan(c, o, plan, s, false, true, false);
+    }
+}
+
 void prepare_tc_kernels() {
     static thread_local int done_device = -1;
     int dev = 0;
@@ -624,6 +910,10 @@ void prepare_tc_kernels() {
     if (done_device == dev) return;
     set_tc_attr<CTA1_THREADS, CTA1_ROUNDS, 2048, 1024, 14, 12>();
     set_tc_attr<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17, 1>();
+    CK(cudaFuncSetAttribute((const void *)k_tc_core<CORE_THREADS, CORE_K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)CORE_SMEM_MAX));
+    CK(cudaFuncSetAttribute((const void *)k_tc_core<CORE_THREADS, CORE_K>,
+                            cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     done_device = dev;
 }
 
@@ -735,7 +1025,10 @@ void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter 
                                                                      s);
         c.launches++;
     }
-    if (plan.nverts[5]) {
+    if (plan.nverts[5] && plan.core_n && !labels.labels) {
+        launch_tc_core(o, plan, 5, plan.core_lcap, tcount, flag, ctr + 2, s);
+        c.launches++;
+    } else if (plan.nverts[5]) {
         launch_tc_cta<CTA2_THREADS, CTA2_ROUNDS, 16384, 8192, 17, 1>(o, plan, 5, labels, tcount, flag, ctr + 2, 152, s);
         c.launches++;
     }

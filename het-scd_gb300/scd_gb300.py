@@ -19,7 +19,7 @@ OK = 0
 ERRORS = {-1: "SCD_ERR_ARG", -2: "SCD_ERR_CUDA", -3: "SCD_ERR_OOM", -4: "SCD_ERR_STATE",
           -5: "SCD_ERR_FORMAT", -6: "SCD_ERR_TIMEOUT", -7: "SCD_ERR_LIMIT"}
 INVALID_LABEL = 0xFFFFFFFF
-FLAG_PROFILE, FLAG_PEXT_TREE, FLAG_NO_GRAPHS, FLAG_TC_OUT_ONLY, FLAG_PRIORITY = 1, 2, 4, 8, 16
+FLAG_PROFILE, FLAG_PEXT_TREE, FLAG_NO_GRAPHS, FLAG_TC_OUT_ONLY, FLAG_PRIORITY, FLAG_TC_HASH = 1, 2, 4, 8, 16, 32
 PHASES = ("parse", "convert", "tc", "partition", "improve", "stats", "wcc_tc", "wcc")
 
 

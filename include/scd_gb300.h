@@ -50,6 +50,9 @@ extern "C" {
 #define SCD_FLAG_PRIORITY 16u     /* the context's streams get the device's highest priority:
                                      their pending thread blocks are scheduled before those of
                                      other contexts (latency-sensitive work beside bulk work) */
+#define SCD_FLAG_TC_HASH 32u      /* preprocessing triangle count of long out-lists by the
+                                     shared hash-table kernels instead of the exact core-bitmap
+                                     kernel; same results */
 
 typedef struct scd_ctx scd_ctx;
 

@@ -279,6 +279,42 @@ def test_in_list_units_agree_with_out_list_counting(engine, make):
         e2.close()
 
 
+def _dense_block(n=1600, p=0.8, seed=11):
+    # out-degrees beyond 1024: centres of the second CTA bucket (1024, 8192]
+    rng = np.random.default_rng(seed)
+    iu, ju = np.triu_indices(n, 1)
+    keep = rng.random(iu.size) < p
+    return np.stack([iu[keep], ju[keep]], axis=1).astype(np.uint32)
+
+
+@pytest.mark.parametrize("out_only", [False, True], ids=["in-lists", "out-only"])
+@pytest.mark.parametrize("kind,make", [
+    ("rmat16", lambda: scdgen.rmat(16, 16, seed=7)),
+    ("chunglu60k", lambda: scdgen.chunglu(60_000, 2.1, 5.0, 5000.0, 0.2, 10, 200, seed=5)),
+    ("planted20k", lambda: scdgen.planted(20_000, 30.0, 0.3, 20, 400, seed=3)),
+    ("dense1600", _dense_block),
+], ids=lambda v: v if isinstance(v, str) else "")
+def test_core_bitmap_kernel_agrees_with_hash_kernels(kind, make, out_only):
+    # the exact core-bitmap CTA kernel (default) and the shared hash-table CTA
+    # kernels count the same triangles: the same graph bytes
+    pairs = make()
+    base = S.FLAG_TC_OUT_ONLY if out_only else 0
+    e1, e2 = S.Engine(0, flags=base), S.Engine(0, flags=base | S.FLAG_TC_HASH)
+    try:
+        e1.convert_edges(pairs)
+        e2.convert_edges(pairs)
+        assert e1.graph_bytes() == e2.graph_bytes()
+    finally:
+        e1.close()
+        e2.close()
+
+
+def test_core_bitmap_kernel_against_oracle_on_dense_block(engine):
+    pairs = _dense_block()
+    engine.convert_edges(pairs)
+    assert engine.graph_bytes() == O.convert(pairs)[0].to_bytes()
+
+
 def test_autotune_keeps_results():
     # every split the autotuner may pick counts the same triangles
     pairs = scdgen.chunglu(40_000, 2.1, 5.0, 3000.0, 0.2, 10, 200, seed=9)
