@@ -772,7 +772,8 @@ def bench_plain(S, args, world, rank, local, dist):
                          "note": "from the edge-list text in pinned host memory: device parse + preprocessing + SCD + labels"},
             "gpu_launches": launches,
             "phases_ms": {p: round(v[0], 3) for p, v in prof.items()},
-            "roofline": {"kernel": "k_tc_warp + k_tc_cta (preprocessing triangle counting)", "bound": "hbm",
+            "roofline": {"kernel": "k_tc_core + k_tc_cta + k_tc_warp + k_tc_small (preprocessing triangle counting)",
+                         "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "algorithmic_bytes": b_tc, "ms_per_launch": tc_avg,
                          "traffic": traffic},
