@@ -640,6 +640,9 @@ int scd_create(scd_ctx **out, int device_id, int work_group_size, unsigned flags
         }
         CK(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, prio));
         CK(cudaStreamCreateWithPriority(&c.side, cudaStreamNonBlocking, prio));
+        CK(cudaStreamCreateWithPriority(&c.aux, cudaStreamNonBlocking, prio));
+        CK(cudaEventCreateWithFlags(&c.aux_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c.aux_join, cudaEventDisableTiming));
         CK(cudaMalloc((void **)&c.work_counter, 64));
         CK(cudaMallocHost((void **)&c.wcc_host, sizeof(double)));
         CK(cudaMallocHost((void **)&c.host_u32, 2 * sizeof(uint32_t)));
@@ -673,6 +676,12 @@ void scd_destroy(scd_ctx *ctx) {
     if (c.pext_ready) cudaEventDestroy(c.pext_ready);
     if (c.stream) cudaStreamDestroy(c.stream);
     if (c.side) cudaStreamDestroy(c.side);
+    if (c.aux) {
+        cudaStreamSynchronize(c.aux);
+        cudaStreamDestroy(c.aux);
+    }
+    if (c.aux_fork) cudaEventDestroy(c.aux_fork);
+    if (c.aux_join) cudaEventDestroy(c.aux_join);
     delete ctx;
 }
 

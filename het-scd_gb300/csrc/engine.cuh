@@ -199,6 +199,8 @@ struct Ctx {
     double alpha = 1.0;
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;
+    cudaStream_t aux = nullptr;                        // improve: the hub kernel beside the other classes
+    cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
     std::string err;
     uint64_t launches = 0;
     uint32_t tc_small = 32, tc_b0 = 64, tc_b1 = 1024;   // triangle-counting bucket splits (autotuned)

@@ -814,6 +814,19 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
     ImproveArgs a{g.indices, g.adj, labels, st, c.pin64, c.civ, c.b.p_ext, c.b.pe32, c.b.gid,
                   frozen_graphs ? c.b.active : nullptr, c.alpha, next};
     const DegreeClasses &k = g.cls;
+    // the hub class (one CTA per vertex of degree > 4096, bound by the latency of its
+    // global-memory tables) runs on the auxiliary stream beside the other classes;
+    // the classes decide disjoint vertices from the same labels and statistics
+    const bool fork = k.count[7] && c.aux;
+    if (fork) {
+        CK(cudaEventRecord(c.aux_fork, s));
+        CK(cudaStreamWaitEvent(c.aux, c.aux_fork, 0));
+        k_improve_global<<<grid_for(k.count[7], 1, 152 * 2), GLOBAL_THREADS, 0, c.aux>>>(k.list[7], k.count[7], a,
+                                                                                        c.big_tables, g.big_table_off);
+        CK_LAUNCH("k_improve_global");
+        CK(cudaEventRecord(c.aux_join, c.aux));
+        c.launches++;
+    }
     if (k.count[0]) {
         k_improve_group<8><<<grid_for((uint64_t)k.count[0] * 8, TPB, GROUP_GRID), TPB, 0, s>>>(k.list[0], k.count[0], a);
         CK_LAUNCH("k_improve_group8");
@@ -847,7 +860,9 @@ void improve(Ctx &c, const uint32_t *labels, const Stats &st, uint32_t *next, bo
         launch_cta<512, 8192>(k.list[6], k.count[6], a, s, 152 * 2);
         c.launches++;
     }
-    if (k.count[7]) {
+    if (fork) {
+        CK(cudaStreamWaitEvent(s, c.aux_join, 0));
+    } else if (k.count[7]) {
         k_improve_global<<<grid_for(k.count[7], 1, 152 * 2), GLOBAL_THREADS, 0, s>>>(k.list[7], k.count[7], a,
                                                                                     c.big_tables, g.big_table_off);
         CK_LAUNCH("k_improve_global");

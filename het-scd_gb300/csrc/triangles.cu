@@ -996,6 +996,7 @@ void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter 
     uint32_t *ctr = c.work_counter;
     CK(cudaMemsetAsync(ctr, 0, 16, s));
     const Dir dir{plan.dir_lo, plan.dir_hi, plan.dir_amin};
+    const bool core = plan.nverts[5] && plan.core_n && !labels.labels;
     if (plan.nverts[0]) {
         k_tc_small<8><<<grid_for((uint64_t)plan.nverts[0] * 8, 256, 152 * 8), 256, 0, s>>>(
             o, plan.verts[0], plan.nverts[0], dir, labels, tcount, flag);
@@ -1025,7 +1026,7 @@ void count_triangles(Ctx &c, const Oriented &o, const TcPlan &plan, LabelFilter 
                                                                      s);
         c.launches++;
     }
-    if (plan.nverts[5] && plan.core_n && !labels.labels) {
+    if (core) {
         launch_tc_core(o, plan, 5, plan.core_lcap, tcount, flag, ctr + 2, s);
         c.launches++;
     } else if (plan.nverts[5]) {
