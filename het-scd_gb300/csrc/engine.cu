@@ -645,7 +645,7 @@ int scd_create(scd_ctx **out, int device_id, int work_group_size, unsigned flags
         CK(cudaEventCreateWithFlags(&c.aux_join, cudaEventDisableTiming));
         CK(cudaMalloc((void **)&c.work_counter, 64));
         CK(cudaMallocHost((void **)&c.wcc_host, sizeof(double)));
-        CK(cudaMallocHost((void **)&c.host_u32, 2 * sizeof(uint32_t)));
+        CK(cudaMallocHost((void **)&c.host_u32, 32 * sizeof(uint32_t)));
     } catch (const Error &e) {
         scd_destroy(ctx);
         return e.status;

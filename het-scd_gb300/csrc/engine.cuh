@@ -154,14 +154,15 @@ struct TcPlan {
 };
 struct Ctx;
 // in_lists: also in-list centres (b-centric edges) in the CTA buckets
-// core_split: the upper CTA bucket starts at tc_core (the core-bitmap kernel's
-// split, for a plan that gets a core map) instead of tc_b1
+// core_from > 0: the upper CTA bucket starts at that out-degree (the core-bitmap
+// kernel's split, for a plan that gets a core map) instead of tc_b1
 void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists,
-             bool core_split = false);
-// builds the core map of the upper CTA bucket for out-lists o.adj[0..slots)
-// (symmetric degree of v = o.len[v] + o.in_len(v)); leaves core_n = 0 when the
-// core's bitmap would not fit the core kernel's shared memory
-void tc_core_map(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s);
+             uint32_t core_from = 0);
+// builds the core map of the upper CTA bucket (from plan.cta_hi) for out-lists
+// o.adj[0..slots) (symmetric degree of v = o.len[v] + o.in_len(v)); core_n: the
+// core's size, lcap: the bucket's longest out-list (both counted beforehand)
+void tc_core_map(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, uint32_t core_n, uint32_t lcap,
+                 cudaStream_t s);
 // the plan of a full count (preprocessing) over out-lists o.adj[0..slots) with in-list
 // centres: the core split and its core map, or the hash kernels' split
 void tc_plan_counting(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s);
@@ -204,7 +205,6 @@ struct Ctx {
     std::string err;
     uint64_t launches = 0;
     uint32_t tc_small = 32, tc_b0 = 64, tc_b1 = 1024;   // triangle-counting bucket splits (autotuned)
-    uint32_t tc_core = 256;   // preprocessing count: out-degree from which the core-bitmap kernel runs
     uint32_t tc_amin = 0;   // b-centric edges need d+(a) > tc_amin (autotuned; at most tc_small)
 
     Graph g;
@@ -228,7 +228,7 @@ struct Ctx {
     uint32_t *int_adj = nullptr;      // and the internal out-lists at the CSR offsets (2m)
     TcPlan wplan;                     // triangle-counting plan of the resident graph
     double *wcc_part = nullptr, *wcc_host = nullptr;
-    uint32_t *host_u32 = nullptr;     // pinned: the active-graph count of an iteration
+    uint32_t *host_u32 = nullptr;     // pinned: the active-graph count of an iteration [0, 2), planning words [2, 32)
     char *io_buf[2] = {};             // pinned pieces of a graph file on its way to the device
     cudaEvent_t io_done[2] = {};
     uint32_t *big_tables = nullptr;   // global hash tables of the last degree bucket

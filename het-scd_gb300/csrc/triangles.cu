@@ -37,10 +37,12 @@
 // grouped by out-degree into buckets so that each kernel's shared memory
 // matches its lists.
 //
-// The preprocessing count takes its upper CTA bucket (out-degree > 256, where
+// The preprocessing count takes its upper CTA bucket (out-degree > T, where
 // nearly all the work of skewed graphs lies) with an exact bitmap instead of a
 // hash table: those centres' out-lists all lie among the vertices of degree >
-// 256, numbered densely, so a small shared bitmap holds each one (k_tc_core).
+// T, numbered densely, so a small shared bitmap holds each one (k_tc_core).
+// T is the lowest of 64, 128, 256, 512, 1024 whose core has at most 128K
+// vertices (R-MAT scale 22: 128; Chung-Lu 8M: 256).
 #include "engine.cuh"
 
 namespace scd {
@@ -693,6 +695,8 @@ k_tc_core(Oriented o, const uint32_t *__restrict__ cpad, const uint32_t *__restr
 
 constexpr int CORE_THREADS = 256, CORE_K = 2;
 constexpr size_t CORE_SMEM_MAX = 200 * 1024;   // below the 227 KB opt-in limit with the static part
+// core size (vertices) whose bitmap and position table (24 KB) leave room for six CTAs per SM
+constexpr uint32_t CORE_BUDGET = 128 * 1024;
 
 inline size_t tc_core_smem(uint32_t kwords, uint32_t lcap) {
     return (size_t)kwords * 4 + (size_t)(lcap + 1) / 2 * 4 + ((size_t)kwords * 2 + 3) / 4 * 4;
@@ -767,13 +771,32 @@ struct CoreFlag {
     __device__ uint32_t operator[](size_t v) const { return o.len[v] + o.in_len((uint32_t)v) > bound; }
 };
 
-// largest out-degree among the centres verts[0..n)
-__global__ void k_max_len(const uint32_t *__restrict__ len, const uint32_t *__restrict__ verts, uint32_t n,
-                          uint32_t *mx) {
-    uint32_t m = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) m = max(m, len[verts[i]]);
-    for (int d = 16; d > 0; d >>= 1) m = max(m, __shfl_xor_sync(FULL, m, d));
-    if ((threadIdx.x & 31) == 0 && m) atomicMax(mx, m);
+// for the candidate core bounds t[j]: cnt[j] = vertices of symmetric degree
+// > t[j] (the core), cnt[K + j] = the largest out-degree in (t[j], 8192] (the
+// upper CTA bucket's longest out-list, which sizes the per-member counts)
+struct CoreBounds {
+    static constexpr int K = 5;
+    uint32_t t[K];
+};
+__global__ void k_core_counts(Oriented o, CoreBounds cb, uint32_t *cnt) {
+    uint32_t m[CoreBounds::K] = {}, mx[CoreBounds::K] = {};
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < o.n; v += gridDim.x * blockDim.x) {
+        const uint32_t len = o.len[v], d = len + o.in_len(v);
+#pragma unroll
+        for (int j = 0; j < CoreBounds::K; j++) {
+            m[j] += d > cb.t[j];
+            if (len > cb.t[j] && len <= 8192u) mx[j] = max(mx[j], len);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < CoreBounds::K; j++) {
+        uint32_t t = warp_sum(m[j]), x = mx[j];
+        for (int d = 16; d > 0; d >>= 1) x = max(x, __shfl_xor_sync(FULL, x, d));
+        if ((threadIdx.x & 31) == 0) {
+            if (t) atomicAdd(cnt + j, t);
+            if (x) atomicMax(cnt + CoreBounds::K + j, x);
+        }
+    }
 }
 
 // padded list length: every list starts on a 16-byte boundary
@@ -802,11 +825,11 @@ __global__ void k_core_pad(Oriented o, const uint32_t *__restrict__ cpos, uint32
 
 }  // namespace
 
-void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists, bool core_split) {
+void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned, bool in_lists, uint32_t core_from) {
     const uint32_t sm = c.tc_small, s16 = sm < 16 ? sm : 16, s8 = sm < 8 ? sm : 8, b0 = c.tc_b0 > sm ? c.tc_b0 : sm;
-    // the core-bitmap kernel takes the upper CTA bucket from tc_core on; the hash
+    // the core-bitmap kernel takes the upper CTA bucket from core_from on; the hash
     // kernels' upper bucket (one CTA per SM, 16K-entry tables) from tc_b1 on
-    const uint32_t b1 = core_split ? (c.tc_core > b0 ? c.tc_core : b0) : c.tc_b1;
+    const uint32_t b1 = core_from ? (core_from > b0 ? core_from : b0) : c.tc_b1;
     const uint32_t bounds[TcPlan::K + 1] = {0, s8, s16, sm, b0, b1, B2, 0xffffffffu};
     const uint32_t per_unit[TcPlan::K] = {1, 1, 1, 32, CTA1_THREADS * CTA1_ROUNDS, CTA2_THREADS * CTA2_ROUNDS, 1};
     const bool split = in_lists && !(c.flags & SCD_FLAG_TC_OUT_ONLY);
@@ -859,48 +882,61 @@ void tc_plan(Ctx &c, const Oriented &o, TcPlan &plan, cudaStream_t s, bool owned
     }
 }
 
-void tc_core_map(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s) {
+void tc_core_map(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, uint32_t core_n, uint32_t lcap,
+                 cudaStream_t s) {
     plan.core_adj = plan.core_beg = nullptr;
     plan.core_n = plan.core_lcap = 0;
     if (o.n == 0 || plan.nverts[5] == 0) return;
-    if (slots + 3ull * o.n >= 0xffffffffull) return;   // the padded layout is indexed in 32 bits
-    DevBuf<uint32_t> cpos((size_t)o.n + 1, s), mx(1, s);
+    const uint64_t padded = slots + 3ull * o.n;   // at most: every list padded by three
+    if (padded >= 0xffffffffull) return;          // the padded layout is indexed in 32 bits
+    DevBuf<uint32_t> cpos((size_t)o.n + 1, s);
     plan.core_beg_buf.alloc((size_t)o.n + 1, s);
+    plan.core_buf.alloc((size_t)padded + 4, s);
     scan_exclusive<uint32_t>(CoreFlag{o, plan.cta_hi}, cpos.get(), o.n, s);
     scan_exclusive<uint32_t>(PadLen{o.len}, plan.core_beg_buf.get(), o.n, s);
-    CK(cudaMemsetAsync(mx.get(), 0, 4, s));
-    k_max_len<<<grid_for(plan.nverts[5], 256, 152 * 4), 256, 0, s>>>(o.len, plan.verts[5], plan.nverts[5], mx.get());
-    CK_LAUNCH("k_max_len");
-    uint32_t h[3] = {0, 0, 0};
-    CK(cudaMemcpyAsync(&h[0], cpos.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&h[1], plan.core_beg_buf.get() + o.n, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(&h[2], mx.get(), 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    const uint32_t core_n = h[0], padded = h[1], lcap = (h[2] + 1) & ~1u;
-    if (tc_core_smem(core_n / 32 + 1, lcap) > CORE_SMEM_MAX) {
-        plan.core_beg_buf.release();
-        return;
-    }
-    plan.core_buf.alloc((size_t)padded + 4, s);
     k_core_pad<<<grid_for((uint64_t)o.n * 32, 256, 152 * 16), 256, 0, s>>>(o, cpos.get(), core_n,
                                                                            plan.core_beg_buf.get(), plan.core_buf.get());
     CK_LAUNCH("k_core_pad");
-    c.launches += 2;
+    c.launches++;
     plan.core_adj = plan.core_buf.get();
     plan.core_beg = plan.core_beg_buf.get();
     plan.core_n = core_n;
-    plan.core_lcap = lcap;
+    plan.core_lcap = (lcap + 1) & ~1u;
 }
 
 void tc_plan_counting(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, cudaStream_t s) {
-    const bool core = !(c.flags & SCD_FLAG_TC_HASH);
-    tc_plan(c, o, plan, s, false, true, core);
-    if (!core) return;
-    tc_core_map(c, o, slots, plan, s);
-    if (plan.core_n == 0 && plan.nverts[5] && plan.cta_hi != c.tc_b1) {   // no map: the hash kernels' split
-        plan = TcPlan();
-        tc_plan(c, o, plan, s, false, true, false);
+    if (c.flags & SCD_FLAG_TC_HASH || o.n == 0) {
+        tc_plan(c, o, plan, s, false, true);
+        return;
     }
+    // the core kernel starts at the lowest candidate bound whose core fits the
+    // bitmap budget (many CTAs per SM), else at the lowest one that fits at all
+    const uint32_t b0 = c.tc_b0 > c.tc_small ? c.tc_b0 : c.tc_small;
+    constexpr int K = CoreBounds::K;
+    CoreBounds cb{};
+    const uint32_t cand[K] = {b0, 128, 256, 512, 1024};
+    for (int j = 0; j < K; j++) cb.t[j] = cand[j] > b0 ? cand[j] : b0;
+    DevBuf<uint32_t> cnt(2 * K, s);
+    CK(cudaMemsetAsync(cnt.get(), 0, 8 * K, s));
+    k_core_counts<<<grid_for(o.n, 256, 152 * 8), 256, 0, s>>>(o, cb, cnt.get());
+    CK_LAUNCH("k_core_counts");
+    c.launches++;
+    uint32_t *h = c.host_u32 + 2;   // pinned planning words
+    CK(cudaMemcpyAsync(h, cnt.get(), 8 * K, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    int pick = -1;
+    for (int j = 0; j < K && pick < 0; j++)
+        if (h[j] <= CORE_BUDGET) pick = j;
+    for (int j = 0; j < K && pick < 0; j++)
+        if (tc_core_smem(h[j] / 32 + 1, h[K + j]) <= CORE_SMEM_MAX) pick = j;
+    if (pick >= 0) {
+        const uint32_t core_n = h[pick], lcap = h[K + pick];
+        tc_plan(c, o, plan, s, false, true, cb.t[pick]);
+        tc_core_map(c, o, slots, plan, core_n, lcap, s);
+        if (plan.core_n || !plan.nverts[5]) return;
+        plan = TcPlan();
+    }
+    tc_plan(c, o, plan, s, false, true);   // no map: the hash kernels' split
 }
 
 void prepare_tc_kernels() {
