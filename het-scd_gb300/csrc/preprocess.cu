@@ -10,7 +10,7 @@
 //  3. degree orientation (u -> v iff (deg v, v) > (deg u, u)), triangles per
 //     vertex and "edge lies on a triangle" flags (triangles.cu); tri = 2 x the
 //     vertex's triangles, tri_deg = number of flagged edges (src/convert.cpp:271-340);
-//  4. triangle-free edges dropped and vertices ranked by (tri_deg, id)
+//  4. triangle-free edges dropped and the kept vertices ranked by (tri_deg, id)
 //     descending, degree-0 vertices trimmed (src/convert.cpp:342-414);
 //  5. the final symmetric CSR: rows of the kept edges in rank ids, placed by
 //     the known row lengths (tri_deg) and sorted row by row (src/convert.cpp:417-455).
@@ -157,28 +157,30 @@ __global__ void k_tri_from_count(const uint32_t *__restrict__ tcount, uint32_t n
         tri[v] = (int32_t)(2u * tcount[v]);
 }
 
-// key = ((2^32-1 - tri_deg) << k) | (2^k-1 - v): ascending = (tri_deg, v) descending
-__global__ void k_degree_keys(const int32_t *__restrict__ tri_deg, uint32_t n, int k, uint64_t *keys,
-                              uint32_t *vals) {
+// the kept vertices (tri_deg > 0) at their id-order positions kscan[v], with the
+// key ((maxd - tri_deg) << k) | (2^k-1 - v): ascending = (tri_deg, v) descending
+__global__ void k_kept_keys(const int32_t *__restrict__ tri_deg, uint32_t n, const uint32_t *__restrict__ kscan,
+                            uint32_t maxd, int k, uint64_t *keys, uint32_t *vals) {
     const uint64_t vmax = (1ull << k) - 1;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        keys[v] = ((uint64_t)(0xffffffffu - (uint32_t)tri_deg[v]) << k) | (vmax - v);
-        vals[v] = v;
+        const int32_t d = tri_deg[v];
+        if (d > 0) {
+            const uint32_t i = kscan[v];
+            keys[i] = ((uint64_t)(maxd - (uint32_t)d) << k) | (vmax - v);
+            vals[i] = v;
+        }
     }
 }
 
-// final id = number of kept vertices before v in the sorted order
-__global__ void k_rank_of(const uint32_t *__restrict__ order, uint32_t n, const int32_t *__restrict__ tri,
-                          const int32_t *__restrict__ tri_deg, const uint32_t *__restrict__ kscan, uint32_t *rank,
-                          int32_t *tri_out, int32_t *tri_deg_out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t v = order[i];
-        if (tri_deg[v] > 0) {
-            const uint32_t r = kscan[i];
-            rank[v] = r;
-            tri_out[r] = tri[v];
-            tri_deg_out[r] = tri_deg[v];
-        }
+// final id = position in the sorted order of the kept vertices
+__global__ void k_rank_of(const uint32_t *__restrict__ order, uint32_t n2, const int32_t *__restrict__ tri,
+                          const int32_t *__restrict__ tri_deg, uint32_t *rank, int32_t *tri_out,
+                          int32_t *tri_deg_out) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n2; r += gridDim.x * blockDim.x) {
+        const uint32_t v = order[r];
+        rank[v] = r;
+        tri_out[r] = tri[v];
+        tri_deg_out[r] = tri_deg[v];
     }
 }
 
@@ -297,13 +299,13 @@ __global__ void k_graph_of_order(const uint32_t *__restrict__ order, uint32_t n,
         keys[i] = segment_of32(ren_off, G, order[i]);
 }
 
-struct KeptAt {
-    const uint32_t *order;
+struct Kept {
     const int32_t *tri_deg;
-    __device__ uint32_t operator[](size_t i) const { return tri_deg[order[i]] > 0; }
+    __device__ uint32_t operator[](size_t v) const { return tri_deg[v] > 0; }
 };
 
-// first final id of every graph: kept vertices before the graph's first sorted position
+// first final id of every graph: kept vertices before the graph's first renamed id
+// (renamed ids, and so the kept vertices in id order, are graph-contiguous)
 __global__ void k_final_offsets(uint32_t G, const uint32_t *__restrict__ ren_off, const uint32_t *__restrict__ kscan,
                                 uint32_t *fin_off) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x)
@@ -470,21 +472,31 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     obeg.release();
     olen.release();
 
-    // 4. rank by (tri_deg, id) descending within each graph; trim vertices
-    //    without triangle edges; final ids count the kept vertices in that order
-    DevBuf<uint64_t> dkeys(n1, s);
-    DevBuf<uint32_t> order(n1, s), rank(n1, s), kscan(n1 + 1, s);
-    k_degree_keys<<<grid_for(n1, TPB), TPB, 0, s>>>(tdeg1.get(), n1, k1, dkeys.get(), order.get());
-    CK_LAUNCH("k_degree_keys");
-    radix_sort<uint64_t>(dkeys.get(), order.get(), n1, 0, 32 + k1, s);
+    // 4. rank by (tri_deg, id) descending within each graph; vertices without
+    //    triangle edges are trimmed, so only the kept ones are sorted (those with
+    //    tri_deg 0 would sort after all of them), on keys as wide as the largest
+    //    tri_deg needs
+    DevBuf<uint32_t> kscan(n1 + 1, s), dmax(1, s);
+    scan_exclusive<uint32_t>(Kept{tdeg1.get()}, kscan.get(), n1, s);
+    CK(cudaMemsetAsync(dmax.get(), 0, 4, s));
+    k_reduce_max<uint32_t><<<grid_for(n1, TPB, 152 * 8), TPB, 0, s>>>((const uint32_t *)tdeg1.get(), n1, dmax.get());
+    CK_LAUNCH("k_reduce_max");
+    uint32_t *hk = c.host_u32 + 2;   // pinned words: kept vertices, largest tri_deg
+    CK(cudaMemcpyAsync(hk, kscan.get() + n1, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(hk + 1, dmax.get(), 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const uint32_t n2 = hk[0], maxd = hk[1];
+    DevBuf<uint64_t> dkeys(n2 ? n2 : 1, s);
+    DevBuf<uint32_t> order(n2 ? n2 : 1, s), rank(n1, s);
+    k_kept_keys<<<grid_for(n1, TPB), TPB, 0, s>>>(tdeg1.get(), n1, kscan.get(), maxd, k1, dkeys.get(), order.get());
+    CK_LAUNCH("k_kept_keys");
+    radix_sort<uint64_t>(dkeys.get(), order.get(), n2, 0, k1 + ceil_log2((uint64_t)maxd + 1), s);
     if (NG > 1) {   // graph-major (stable): each graph's vertices stay contiguous
-        k_graph_of_order<<<grid_for(n1, TPB), TPB, 0, s>>>(order.get(), n1, ren_off.get(), NG, dkeys.get());
+        k_graph_of_order<<<grid_for(n2 ? n2 : 1, TPB), TPB, 0, s>>>(order.get(), n2, ren_off.get(), NG, dkeys.get());
         CK_LAUNCH("k_graph_of_order");
-        radix_sort<uint64_t>(dkeys.get(), order.get(), n1, 0, ceil_log2(NG), s);
+        radix_sort<uint64_t>(dkeys.get(), order.get(), n2, 0, ceil_log2(NG), s);
     }
     dkeys.release();
-    scan_exclusive<uint32_t>(KeptAt{order.get(), tdeg1.get()}, kscan.get(), n1, s);
-    const uint32_t n2 = read_scalar(kscan.get() + n1, s);
 
     // 5. final symmetric CSR in rank ids: row lengths are the kept edges (tri_deg), rows filled then sorted
     Graph &g = c.g;
@@ -492,8 +504,8 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     g.indices = c.alloc<uint32_t>((size_t)n2 + 1);
     g.tri = c.alloc<int32_t>(n2);
     g.tri_deg = c.alloc<int32_t>(n2);
-    k_rank_of<<<grid_for(n1, TPB), TPB, 0, s>>>(order.get(), n1, tri1.get(), tdeg1.get(), kscan.get(), rank.get(),
-                                               g.tri, g.tri_deg);
+    k_rank_of<<<grid_for(n2 ? n2 : 1, TPB), TPB, 0, s>>>(order.get(), n2, tri1.get(), tdeg1.get(), rank.get(), g.tri,
+                                                       g.tri_deg);
     CK_LAUNCH("k_rank_of");
     scan_exclusive<uint32_t>(DegreeOf{g.tri_deg}, g.indices, n2, s);
     const uint32_t m2 = read_scalar(g.indices + n2, s) / 2;
