@@ -358,18 +358,7 @@ def bench_batched(S, device, args):
     sizes = [g.shape[0] for g in graphs]
     records = int(sum(sizes))
     groups = split_batches(sizes, args.batch_records)
-    # the host edge lists live in pinned memory, as a request buffer of a serving host
-    # would: both arms copy them with DMA at full speed.  (From pageable memory the
-    # device reads them through address translation, whose speed drifted down run
-    # after run in one process: 0.64 -> 0.99 s for the same 14.5 GB.)
-    host = torch.empty(2 * records, dtype=torch.int32, pin_memory=True)
-    hv = host.numpy().view(np.uint32)
-    off = 0
-    for i, g in enumerate(graphs):
-        n2 = 2 * g.shape[0]
-        hv[off:off + n2] = g.reshape(-1)
-        graphs[i] = hv[off:off + n2].reshape(-1, 2)
-        off += n2
+    host = pin_lists(graphs)   # both arms read the edge lists from pinned memory
     labels_out = torch.empty(records, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     eng = S.Engine(device)
     eng.batch_convert([graphs[i] for i in groups[0]])
@@ -470,6 +459,27 @@ def _gen_request(spec):
     return scdgen.rmat(size, 16, 0.57, 0.19, 0.19, seed=seed)
 
 
+def pin_lists(graphs):
+    """Moves the (E, 2) uint32 edge lists into one pinned host buffer, as a serving
+    host's request buffer would hold them, and replaces them by views into it: the
+    device then copies them with DMA at full speed.  (From pageable memory the device
+    reads them through address translation, whose speed drifted down run after run:
+    0.64 -> 0.99 s for the same 14.5 GB in one process, and served capacity fell by
+    half over a sequence of processes on one box.)  Returns the buffer (keep it alive)."""
+    import numpy as np
+    import torch
+    records = int(sum(g.shape[0] for g in graphs))
+    host = torch.empty(max(2 * records, 1), dtype=torch.int32, pin_memory=True)
+    hv = host.numpy().view(np.uint32)
+    off = 0
+    for i, g in enumerate(graphs):
+        n2 = 2 * g.shape[0]
+        hv[off:off + n2] = g.reshape(-1)
+        graphs[i] = hv[off:off + n2].reshape(-1, 2)
+        off += n2
+    return host
+
+
 def per_graph_loop(S, device, graphs):
     """The plain per-graph loop: one engine, each graph converted, run to
     convergence and its labels copied out before the next (the reference's one
@@ -510,6 +520,7 @@ def bench_served(S, device, args):
     t0 = time.time()
     reqs = generate(_gen_request, specs)
     gen_s = time.time() - t0
+    pinned = pin_lists(reqs)   # requests arrive in a pinned receive buffer, for the loop and the server
     loop_s, loop_out = per_graph_loop(S, device, reqs)
     srv = serve.Server(device, converters=args.serve_converters, budget_bytes=120e9, max_batch=64)
     for r in [srv.submit(reqs[i]) for i in range(min(8, len(reqs)))]:   # warm-up
@@ -552,6 +563,7 @@ def bench_served(S, device, args):
              for k, ln in enumerate(srv.lanes)]
     conv_ms = [b[1] * 1e3 for b in srv.batches]
     srv.close()
+    del pinned   # the request buffer outlives the loop and the server
     lat = [h.latency * 1e3 for h in handles]
     span = end - t
     sizes = [b[0] for b in srv.batches]
@@ -576,6 +588,7 @@ def bench_served(S, device, args):
             "converters": args.serve_converters, "budget_gb": 120, "peak_admitted_gb": srv.peak_in_use / 1e9,
             "conversion_batches": len(sizes), "mean_conversion_batch": float(np.mean(sizes)) if sizes else 0.0,
             "conversion_ms_p50": serve.percentile(conv_ms, 50), "lanes": lanes,
+            "timing": "host wall clock, requests in a pinned host buffer, labels out to the host",
             "generate_s": round(gen_s, 1)}
 
 

@@ -913,6 +913,14 @@ void tc_plan_counting(Ctx &c, const Oriented &o, uint64_t slots, TcPlan &plan, c
     // bitmap budget (many CTAs per SM), else at the lowest one that fits at all
     const uint32_t b0 = c.tc_b0 > c.tc_small ? c.tc_b0 : c.tc_small;
     constexpr int K = CoreBounds::K;
+    if (o.n <= CORE_BUDGET) {   // every core fits the budget: the lowest split, no host read
+        tc_plan(c, o, plan, s, false, true, b0);
+        tc_core_map(c, o, slots, plan, o.n, B2, s);   // core_n <= n; counts sized for the cap
+        if (plan.core_n || !plan.nverts[5]) return;
+        plan = TcPlan();
+        tc_plan(c, o, plan, s, false, true);
+        return;
+    }
     CoreBounds cb{};
     const uint32_t cand[K] = {b0, 128, 256, 512, 1024};
     for (int j = 0; j < K; j++) cb.t[j] = cand[j] > b0 ? cand[j] : b0;
