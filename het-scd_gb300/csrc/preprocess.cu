@@ -5,11 +5,12 @@
 //     every raw id (atomicMin over the 2E endpoint slots), a bitmap of those
 //     positions and a popcount prefix give each id its rank of first appearance;
 //  2. both directions of every renamed non-loop pair placed by a counting sort
-//     on the row, every row sorted and its repeated values dropped (csr.cu):
-//     the de-duplicated symmetric CSR (src/convert.cpp:252-268 + 417-463);
-//  3. degree orientation (u -> v iff (deg v, v) > (deg u, u)), triangles per
-//     vertex and "edge lies on a triangle" flags (triangles.cu); tri = 2 x the
-//     vertex's triangles, tri_deg = number of flagged edges (src/convert.cpp:271-340);
+//     on the row, every row sorted and its repeated values marked (csr.cu): the
+//     de-duplicated symmetric rows (src/convert.cpp:252-268 + 417-463);
+//  3. degree orientation (u -> v iff (deg v, v) > (deg u, u)) read straight off
+//     those rows into out-lists and in-lists, triangles per vertex and "edge lies
+//     on a triangle" flags (triangles.cu); tri = 2 x the vertex's triangles,
+//     tri_deg = number of flagged edges (src/convert.cpp:271-340);
 //  4. triangle-free edges dropped and the kept vertices ranked by (tri_deg, id)
 //     descending, degree-0 vertices trimmed (src/convert.cpp:342-414);
 //  5. the final symmetric CSR: rows of the kept edges in rank ids, placed by
@@ -82,61 +83,155 @@ __global__ void k_pair_fill(const uint32_t *__restrict__ pairs, uint64_t count, 
     }
 }
 
-struct NotInvalid {
-    const uint32_t *v;
-    __device__ uint32_t operator[](size_t i) const { return v[i] != INVALID; }
+// u -> v iff (deg v, v) > (deg u, u): the degree orientation
+__device__ __forceinline__ bool is_out(uint32_t u, uint32_t du, uint32_t v, uint32_t dv) {
+    return dv > du || (dv == du && v > u);
+}
+
+// rows of more than LONG_ROW entries (repeats included) go to a CTA each
+constexpr uint32_t LONG_ROW = 4096;
+constexpr int LONG_THREADS = 512;
+
+struct LongRow {
+    const uint32_t *off;
+    __device__ uint32_t operator[](size_t u) const { return off[u + 1] - off[u] > LONG_ROW; }
 };
 
-__global__ void k_compact_vals(const uint32_t *__restrict__ vals, uint32_t count, const uint32_t *__restrict__ pos,
-                               uint32_t *out) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const uint32_t v = vals[i];
-        if (v != INVALID) out[pos[i]] = v;
+__global__ void k_long_list(const uint32_t *__restrict__ off, uint32_t n, const uint32_t *__restrict__ lpos,
+                            uint32_t *longs) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+        if (off[u + 1] - off[u] > LONG_ROW) longs[lpos[u]] = u;
+}
+
+// out-slots of every short de-duplicated row (one warp per row; INVALID holes skipped)
+__global__ void k_row_out_count(const uint32_t *__restrict__ off, uint32_t n, const uint32_t *__restrict__ vals,
+                                const uint32_t *__restrict__ deg, uint32_t *olen) {
+    const uint32_t lane = threadIdx.x & 31, warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
+        const uint32_t b = off[u], e = off[u + 1];
+        if (e - b > LONG_ROW) continue;
+        const uint32_t du = deg[u];
+        uint32_t c = 0;
+        for (uint32_t i = b + lane; i < e; i += 32) {
+            const uint32_t v = vals[i];
+            if (v != INVALID && is_out(u, du, v, deg[v])) c++;
+        }
+        c = warp_sum(c);
+        if (lane == 0) olen[u] = c;
     }
 }
 
-// rows[t] = r for every slot t of row r
-__global__ void k_fill_rows(const uint32_t *__restrict__ ind, uint32_t nrows, uint32_t *rows) {
-    const int lane = threadIdx.x & 31;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < nrows; r += warps)
-        for (uint32_t t = ind[r] + lane; t < ind[r + 1]; t += 32) rows[t] = r;
+// the same for the long rows, one CTA per row
+__global__ void __launch_bounds__(LONG_THREADS)
+k_long_out_count(const uint32_t *__restrict__ off, const uint32_t *__restrict__ longs, const uint32_t *__restrict__ nlong,
+                 const uint32_t *__restrict__ vals, const uint32_t *__restrict__ deg, uint32_t *olen) {
+    __shared__ uint32_t wsum[LONG_THREADS / 32];
+    const uint32_t nl = *nlong, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t k = blockIdx.x; k < nl; k += gridDim.x) {
+        const uint32_t u = longs[k], du = deg[u], e = off[u + 1];
+        uint32_t c = 0;
+        for (uint32_t i = off[u] + threadIdx.x; i < e; i += LONG_THREADS) {
+            const uint32_t v = vals[i];
+            if (v != INVALID && is_out(u, du, v, deg[v])) c++;
+        }
+        c = warp_sum(c);
+        if (lane == 0) wsum[w] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int j = 0; j < LONG_THREADS / 32; j++) t += wsum[j];
+            olen[u] = t;
+        }
+        __syncthreads();
+    }
 }
 
-struct IsOut {
-    const uint32_t *rows, *cols, *indices;
-    __device__ uint32_t operator[](size_t i) const {
-        uint32_t u = rows[i], v = cols[i];
-        uint32_t du = indices[u + 1] - indices[u], dv = indices[v + 1] - indices[v];
-        return dv > du || (dv == du && v > u);
-    }
+struct InCount {   // in-slots of row u: its distinct values that are not out-slots
+    const uint32_t *deg, *olen;
+    __device__ uint32_t operator[](size_t u) const { return deg[u] - olen[u]; }
 };
 
-// out-slots (u, v) to orow/ocol at pos[i]; in-slots (v -> u) to icol at i - pos[i]
-// (both keep the row order, so out- and in-lists stay sorted)
-__global__ void k_orient(const uint32_t *__restrict__ rows, const uint32_t *__restrict__ cols,
-                         const uint32_t *__restrict__ indices, uint32_t count,
-                         const uint32_t *__restrict__ pos, uint32_t *orow, uint32_t *ocol, uint32_t *icol) {
-    IsOut f{rows, cols, indices};
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        if (f[i]) {
-            orow[pos[i]] = rows[i];
-            ocol[pos[i]] = cols[i];
-        } else {
-            icol[i - pos[i]] = cols[i];
+// out-slots (u, v) of the short rows to orow/ocol from obeg[u] on, in-slots (v -> u)
+// to icol from ibeg[u] on, both in row order (so out- and in-lists stay sorted)
+__global__ void k_row_orient(const uint32_t *__restrict__ off, uint32_t n, const uint32_t *__restrict__ vals,
+                             const uint32_t *__restrict__ deg, const uint32_t *__restrict__ obeg,
+                             const uint32_t *__restrict__ ibeg, uint32_t *orow, uint32_t *ocol, uint32_t *icol) {
+    const uint32_t lane = threadIdx.x & 31, warps = (gridDim.x * blockDim.x) >> 5;
+    const unsigned lt = lanemask_lt();
+    for (uint32_t u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += warps) {
+        const uint32_t b = off[u], e = off[u + 1];
+        if (e - b > LONG_ROW) continue;
+        const uint32_t du = deg[u];
+        uint32_t ob = obeg[u], ib = ibeg[u];
+        for (uint32_t i0 = b; i0 < e; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const uint32_t v = i < e ? vals[i] : INVALID;
+            const bool valid = v != INVALID, out = valid && is_out(u, du, v, deg[v]);
+            const unsigned mo = __ballot_sync(FULL, out), mi = __ballot_sync(FULL, valid && !out);
+            if (out) {
+                const uint32_t p = ob + __popc(mo & lt);
+                orow[p] = u;
+                ocol[p] = v;
+            } else if (valid) {
+                icol[ib + __popc(mi & lt)] = v;
+            }
+            ob += __popc(mo);
+            ib += __popc(mi);
         }
     }
 }
 
-__global__ void k_out_ranges(const uint32_t *__restrict__ indices, const uint32_t *__restrict__ pos,
-                             uint32_t n, uint32_t *obeg, uint32_t *olen, uint32_t *ibeg, uint32_t *ilen) {
-    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
-        const uint32_t r0 = indices[u], r1 = indices[u + 1], b = pos[r0], e = pos[r1];
-        obeg[u] = b;
-        olen[u] = e - b;
-        ibeg[u] = r0 - b;
-        ilen[u] = (r1 - r0) - (e - b);
+// the same for the long rows: one CTA per row, LONG_THREADS entries at a time,
+// positions from a block scan of the out / in flags
+__global__ void __launch_bounds__(LONG_THREADS)
+k_long_orient(const uint32_t *__restrict__ off, const uint32_t *__restrict__ longs, const uint32_t *__restrict__ nlong,
+              const uint32_t *__restrict__ vals, const uint32_t *__restrict__ deg, const uint32_t *__restrict__ obeg,
+              const uint32_t *__restrict__ ibeg, uint32_t *orow, uint32_t *ocol, uint32_t *icol) {
+    constexpr int NW = LONG_THREADS / 32;
+    __shared__ uint32_t so[NW], si[NW];
+    const uint32_t nl = *nlong, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = lanemask_lt();
+    for (uint32_t k = blockIdx.x; k < nl; k += gridDim.x) {
+        const uint32_t u = longs[k], du = deg[u], e = off[u + 1];
+        uint32_t ob = obeg[u], ib = ibeg[u];
+        for (uint32_t i0 = off[u]; i0 < e; i0 += LONG_THREADS) {
+            const uint32_t i = i0 + threadIdx.x;
+            const uint32_t v = i < e ? vals[i] : INVALID;
+            const bool valid = v != INVALID, out = valid && is_out(u, du, v, deg[v]);
+            const unsigned mo = __ballot_sync(FULL, out), mi = __ballot_sync(FULL, valid && !out);
+            if (lane == 0) {
+                so[w] = __popc(mo);
+                si[w] = __popc(mi);
+            }
+            __syncthreads();
+            uint32_t po = 0, pi = 0, to = 0, ti = 0;   // warps before this one, and the whole chunk
+            for (int j = 0; j < NW; j++) {
+                const uint32_t a = so[j], c = si[j];
+                if (j < (int)w) {
+                    po += a;
+                    pi += c;
+                }
+                to += a;
+                ti += c;
+            }
+            if (out) {
+                const uint32_t p = ob + po + __popc(mo & lt);
+                orow[p] = u;
+                ocol[p] = v;
+            } else if (valid) {
+                icol[ib + pi + __popc(mi & lt)] = v;
+            }
+            ob += to;
+            ib += ti;
+            __syncthreads();   // so / si are rewritten by the next chunk
+        }
     }
+}
+
+__global__ void k_in_len(const uint32_t *__restrict__ deg, const uint32_t *__restrict__ olen, uint32_t n,
+                         uint32_t *ilen) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x)
+        ilen[u] = deg[u] - olen[u];
 }
 
 // tri_deg[v] = number of v's edges that lie on a triangle (src/convert.cpp:327-340)
@@ -416,39 +511,39 @@ void convert_edges(Ctx &c, const uint32_t *pairs_in, uint64_t count, const std::
     CK_LAUNCH("k_pair_fill");
     rename.release();
     sort_rows(c, off1.get(), n1, vals.get(), true, cnt.get(), s);   // cnt := distinct values of each row
-    DevBuf<uint32_t> ind1((size_t)n1 + 1, s);
-    scan_exclusive<uint32_t>((const uint32_t *)cnt.get(), ind1.get(), n1, s);
-    const uint32_t slots1 = read_scalar(ind1.get() + n1, s);
-    DevBuf<uint32_t> rows1(slots1 ? slots1 : 1, s), cols1(slots1 ? slots1 : 1, s);
-    {
-        DevBuf<uint32_t> vpos((size_t)entries + 1, s);
-        scan_exclusive<uint32_t>(NotInvalid{vals.get()}, vpos.get(), entries, s);
-        k_compact_vals<<<grid_for(entries, TPB), TPB, 0, s>>>(vals.get(), entries, vpos.get(), cols1.get());
-        CK_LAUNCH("k_compact_vals");
-    }
+    // 3. degree orientation straight from the sorted rows (repeated values are
+    //    INVALID holes): out-slots per row, their offsets, then out-lists (orow,
+    //    ocol) and in-lists (icol) in row order; a warp per row, a CTA per row of
+    //    more than LONG_ROW entries (a hub's row would be one warp's serial loop)
+    DevBuf<uint32_t> olen(n1, s), obeg((size_t)n1 + 1, s), ibeg((size_t)n1 + 1, s);
+    DevBuf<uint32_t> lpos((size_t)n1 + 1, s), longs(n1, s);
+    scan_exclusive<uint32_t>(LongRow{off1.get()}, lpos.get(), n1, s);
+    k_long_list<<<grid_for(n1, TPB), TPB, 0, s>>>(off1.get(), n1, lpos.get(), longs.get());
+    CK_LAUNCH("k_long_list");
+    k_row_out_count<<<grid_for((uint64_t)n1 * 32, TPB), TPB, 0, s>>>(off1.get(), n1, vals.get(), cnt.get(), olen.get());
+    CK_LAUNCH("k_row_out_count");
+    k_long_out_count<<<152 * 2, LONG_THREADS, 0, s>>>(off1.get(), longs.get(), lpos.get() + n1, vals.get(), cnt.get(),
+                                                      olen.get());
+    CK_LAUNCH("k_long_out_count");
+    scan_exclusive<uint32_t>((const uint32_t *)olen.get(), obeg.get(), n1, s);
+    scan_exclusive<uint32_t>(InCount{cnt.get(), olen.get()}, ibeg.get(), n1, s);
+    const uint32_t m1 = read_scalar(obeg.get() + n1, s);
+    DevBuf<uint32_t> orow(m1 ? m1 : 1, s), ocol(m1 ? m1 : 1, s), icol(m1 ? m1 : 1, s);
+    k_row_orient<<<grid_for((uint64_t)n1 * 32, TPB), TPB, 0, s>>>(off1.get(), n1, vals.get(), cnt.get(), obeg.get(),
+                                                                  ibeg.get(), orow.get(), ocol.get(), icol.get());
+    CK_LAUNCH("k_row_orient");
+    k_long_orient<<<152 * 2, LONG_THREADS, 0, s>>>(off1.get(), longs.get(), lpos.get() + n1, vals.get(), cnt.get(),
+                                                   obeg.get(), ibeg.get(), orow.get(), ocol.get(), icol.get());
+    CK_LAUNCH("k_long_orient");
+    c.launches += 8;
     vals.release();
     off1.release();
+    lpos.release();
+    longs.release();
+    DevBuf<uint32_t> ilen(n1, s);
+    k_in_len<<<grid_for(n1, TPB), TPB, 0, s>>>(cnt.get(), olen.get(), n1, ilen.get());
+    CK_LAUNCH("k_in_len");
     cnt.release();
-    k_fill_rows<<<grid_for((uint64_t)n1 * 32, TPB), TPB, 0, s>>>(ind1.get(), n1, rows1.get());
-    CK_LAUNCH("k_fill_rows");
-    c.launches += 5;
-    const uint32_t m1 = slots1 / 2;
-
-    // 3. degree orientation + triangle counts
-    DevBuf<uint32_t> opos(slots1 + 1, s);
-    scan_exclusive<uint32_t>(IsOut{rows1.get(), cols1.get(), ind1.get()}, opos.get(), slots1, s);
-    DevBuf<uint32_t> orow(m1, s), ocol(m1, s), obeg(n1, s), olen(n1, s);
-    DevBuf<uint32_t> icol(m1 ? m1 : 1, s), ibeg(n1, s), ilen(n1, s);
-    k_orient<<<grid_for(slots1, TPB), TPB, 0, s>>>(rows1.get(), cols1.get(), ind1.get(), slots1, opos.get(),
-                                                  orow.get(), ocol.get(), icol.get());
-    CK_LAUNCH("k_orient");
-    k_out_ranges<<<grid_for(n1, TPB), TPB, 0, s>>>(ind1.get(), opos.get(), n1, obeg.get(), olen.get(), ibeg.get(),
-                                                   ilen.get());
-    CK_LAUNCH("k_out_ranges");
-    opos.release();
-    rows1.release();
-    cols1.release();
-    ind1.release();
     DevBuf<uint32_t> tcount(n1, s);
     DevBuf<uint8_t> oflag(m1, s);
     CK(cudaMemsetAsync(tcount.get(), 0, (size_t)n1 * 4, s));
