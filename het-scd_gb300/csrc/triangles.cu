@@ -534,8 +534,8 @@ constexpr int CTA1_THREADS = 128, CTA1_ROUNDS = 4, CTA2_THREADS = 256, CTA2_ROUN
 // bitmap word w; core numbers ascend with ids, so the position of a member c
 // is pre[c/32] + the popcount of the word's bits below c.  A lookup is one
 // shared load and a bit test: no hash, no probe sequence, no false positives.
-// The core of the upper bucket is small (R-MAT scale 22: 110,035 vertices of
-// degree > 256, a 13 KB bitmap), so many CTAs share an SM.
+// The core of the upper bucket is small (R-MAT scale 22: 110,575 vertices of
+// degree > 128, a 13.5 KB bitmap), so many CTAs share an SM.
 //
 // The walk: THREADS partners per round; every list in the core-number array
 // starts on a 16-byte boundary and is padded with core_n to whole quads, the

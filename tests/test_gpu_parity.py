@@ -290,6 +290,7 @@ def _dense_block(n=1600, p=0.8, seed=11):
 @pytest.mark.parametrize("out_only", [False, True], ids=["in-lists", "out-only"])
 @pytest.mark.parametrize("kind,make", [
     ("rmat16", lambda: scdgen.rmat(16, 16, seed=7)),
+    ("rmat18", lambda: scdgen.rmat(18, 16, seed=9)),   # > 128K vertices: the split chosen from core sizes
     ("chunglu60k", lambda: scdgen.chunglu(60_000, 2.1, 5.0, 5000.0, 0.2, 10, 200, seed=5)),
     ("planted20k", lambda: scdgen.planted(20_000, 30.0, 0.3, 20, 400, seed=3)),
     ("dense1600", _dense_block),
