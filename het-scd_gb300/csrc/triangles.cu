@@ -540,19 +540,19 @@ constexpr int CTA1_THREADS = 128, CTA1_ROUNDS = 4, CTA2_THREADS = 256, CTA2_ROUN
 // The walk: THREADS partners per round; every list in the core-number array
 // starts on a 16-byte boundary and is padded with core_n to whole quads, the
 // quads of the round are flattened by a block scan, and a warp takes 32 x K
-// consecutive quads, lane L every 32nd (one 16-byte load each: 4K items of a
-// lane in flight).  A hit flags the walked slot at once and counts in the
-// member's 16-bit shared count and, per quad, in the partner's shared count.
+// consecutive quads of its own contiguous range, lane L every 32nd (one 16-byte
+// load each: 4K items of a lane in flight).  A hit flags the walked slot at
+// once and counts in the member's shared count and, per quad, in the partner's.
 template <int THREADS, int K>
-__global__ void __launch_bounds__(THREADS)
+__global__ void __launch_bounds__(THREADS, 6)
 k_tc_core(Oriented o, const uint32_t *__restrict__ cpad, const uint32_t *__restrict__ cbeg, uint32_t core_n,
           uint32_t kwords, uint32_t lcap, const uint32_t *__restrict__ verts, const uint32_t *__restrict__ unit_off,
           uint32_t nverts, uint32_t nfwd, uint32_t per_unit, Dir dir, uint32_t *tcount, uint8_t *flag,
           uint32_t *next_unit) {
     extern __shared__ __align__(16) uint32_t sm[];
-    uint32_t *bm = sm;                                    // kwords
-    uint32_t *cnt = bm + kwords;                          // lcap 16-bit counts
-    uint16_t *pre = (uint16_t *)(cnt + (lcap + 1) / 2);   // kwords
+    uint32_t *bm = sm;                           // kwords
+    uint32_t *cnt = bm + kwords;                 // lcap hit counts of the centre's members
+    uint16_t *pre = (uint16_t *)(cnt + lcap);    // kwords
     __shared__ uint32_t qpre[THREADS], sq0[THREADS], sdl[THREADS], sh[THREADS], wsum[THREADS / 32];
     __shared__ uint32_t s_unit, s_total, s_xhits;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -585,7 +585,7 @@ k_tc_core(Oriented o, const uint32_t *__restrict__ cpad, const uint32_t *__restr
                 if (i == 0 || (xc[i - 1] >> 5) != (c >> 5)) pre[c >> 5] = (uint16_t)i;
             }
         }
-        for (uint32_t i = threadIdx.x; i < (xlen + 1) / 2; i += THREADS) cnt[i] = 0;
+        for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) cnt[i] = 0;
         const uint32_t *padj = fwd ? o.adj : o.in_adj();
         const uint32_t pbeg = fwd ? xbeg : o.in_beg(x), plen = fwd ? xlen : o.in_len(x);
         const uint32_t pend = min(plen, (ch + 1) * per_unit);
@@ -622,23 +622,30 @@ k_tc_core(Oriented o, const uint32_t *__restrict__ cpad, const uint32_t *__restr
             sh[threadIdx.x] = 0;
             const uint32_t total = s_total;
             __syncthreads();
-            for (uint32_t t0 = (uint32_t)w * 32 * K; t0 < total; t0 += THREADS * K) {
-                const uint32_t tl = t0 + lane;
-                uint32_t l0 = 0, l1 = THREADS;   // owner of tl: last partner with qpre <= tl
+            // warp w walks its own contiguous range of the round's quads, 32 x K at a
+            // time (lane L every 32nd: coalesced); each lane finds the owner of its first
+            // quad once and then only walks the partner boundaries forward
+            const uint32_t wbeg = (uint32_t)(((uint64_t)total * w) / (THREADS / 32));
+            const uint32_t wend = (uint32_t)(((uint64_t)total * (w + 1)) / (THREADS / 32));
+            uint32_t jb = 0, nxt = 0;
+            if (wbeg + lane < wend) {
+                uint32_t l0 = 0, l1 = THREADS;   // owner: last partner with qpre <= the quad
                 while (l0 < l1) {
                     const uint32_t mid = (l0 + l1) >> 1;
-                    if (qpre[mid] <= tl) l0 = mid + 1;
+                    if (qpre[mid] <= wbeg + lane) l0 = mid + 1;
                     else l1 = mid;
                 }
-                uint32_t jb = l0 - 1;
-                uint32_t nxt = jb + 1 < THREADS ? qpre[jb + 1] : total;
+                jb = l0 - 1;
+                nxt = jb + 1 < THREADS ? qpre[jb + 1] : total;
+            }
+            for (uint32_t t0 = wbeg; t0 < wend; t0 += 32 * K) {
                 uint4 v[K];
                 uint32_t qa[K], own[K];
 #pragma unroll
                 for (int k = 0; k < K; k++) {
-                    const uint32_t t = tl + 32 * k;
+                    const uint32_t t = t0 + lane + 32 * k;
                     own[k] = INVALID;
-                    if (t < total) {
+                    if (t < wend) {
                         while (t >= nxt) {
                             jb++;
                             nxt = jb + 1 < THREADS ? qpre[jb + 1] : total;
@@ -659,7 +666,7 @@ k_tc_core(Oriented o, const uint32_t *__restrict__ cpad, const uint32_t *__restr
                         const uint32_t c = vals[e], wd = bm[c >> 5], bit = c & 31;
                         if ((wd >> bit) & 1u) {
                             const uint32_t r = pre[c >> 5] + __popc(wd & ((1u << bit) - 1u));
-                            if (r < xlen) atomicAdd(&cnt[r >> 1], 1u << ((r & 1) << 4));
+                            if (r < xlen) atomicAdd(&cnt[r], 1u);
                             flag[fo + e] = 1;
                             h++;
                         }
@@ -681,7 +688,7 @@ k_tc_core(Oriented o, const uint32_t *__restrict__ cpad, const uint32_t *__restr
         if (threadIdx.x == 0 && s_xhits) atomicAdd(tcount + x, s_xhits);
         const uint32_t *xa = o.adj + xbeg;
         for (uint32_t i = threadIdx.x; i < xlen; i += THREADS) {
-            const uint32_t cc = (cnt[i >> 1] >> ((i & 1) << 4)) & 0xffffu;
+            const uint32_t cc = cnt[i];
             if (cc) {
                 atomicAdd(tcount + xa[i], cc);
                 flag[xbeg + i] = 1;
@@ -699,7 +706,7 @@ constexpr size_t CORE_SMEM_MAX = 200 * 1024;   // below the 227 KB opt-in limit 
 constexpr uint32_t CORE_BUDGET = 128 * 1024;
 
 inline size_t tc_core_smem(uint32_t kwords, uint32_t lcap) {
-    return (size_t)kwords * 4 + (size_t)(lcap + 1) / 2 * 4 + ((size_t)kwords * 2 + 3) / 4 * 4;
+    return (size_t)kwords * 4 + (size_t)lcap * 4 + ((size_t)kwords * 2 + 3) / 4 * 4;
 }
 
 void launch_tc_core(const Oriented &o, const TcPlan &plan, int k, uint32_t lcap, uint32_t *tcount, uint8_t *flag,
